@@ -1,0 +1,452 @@
+"""Benchmark: deforming-mesh per-frame rebuild + trace on one GB300.
+
+Workload (one "step" = one frame): a 160 x 320 x 2 = 102,400-triangle UV
+sphere (pole caps open) whose 51,520 vertices are displaced on the device by
+0.05*sin(3*p.x + 0.3*frame) along their normals; full uniform-grid rebuild
+(cells per triangle k in {2, 4, 8}); 1024 x 1024 primary camera rays; one
+shadow ray per lit-facing hit toward a point light, traced as any-hit.
+Frames cycle through 20 phases.
+
+Prints ONE JSON line (rank 0).  `value` = (primary + shadow rays) / frame
+time, device-timed with CUDA events on the scene's stream, inputs resident,
+L2 flushed between frames.  `e2e` = the same through the public C ABI with
+host buffers: host-deformed vertices uploaded from pinned memory, synchronous
+build, frame trace, hits + occlusion copied back every frame.
+
+--impl reference times the reference's CPU path (the oracle restatement of
+UniformGridAccStructBuilder + UniformGridAccStruct, compiled here) on the
+host cores on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "grid-rt_gb300"))
+
+from gridrt import scenes  # noqa: E402
+
+FRAMES = 20
+LAMBDAS = (2, 4, 8)
+WIDTH = HEIGHT = 1024
+METRIC = "Mrays/s (primary + shadow, per-frame rebuild included)"
+WORKLOAD = "deforming_sphere_102400tri_1024x1024_shadow"
+
+
+def _peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl"
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            backend = "gloo"
+        else:
+            torch.cuda.set_device(local)
+    except Exception:
+        backend = "gloo"
+    dist.init_process_group(backend=backend)
+    return rank, ws, local, dist
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle restatement of the reference path), bounded sample
+# ---------------------------------------------------------------------------
+def cpu_frame_sample(k: int, frame: int, sample_stride: int, nthreads: int = 0):
+    """Build the frame's grid single-threaded (the reference's build is), trace
+    every `sample_stride`-th primary ray plus the shadow rays of those hits on
+    all host threads; extrapolate to the full frame."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    sc = scenes.deforming_sphere(frame)
+    t0 = time.perf_counter()
+    g = pyoracle.Grid(sc.verts, sc.idx, k)
+    t_build = time.perf_counter() - t0
+    cam = scenes.deforming_sphere_camera(WIDTH, HEIGHT)
+    rays = scenes.camera_rays(cam)[::sample_stride]
+    t0 = time.perf_counter()
+    h = g.trace_closest(rays, nthreads=nthreads)
+    t_prim = time.perf_counter() - t0
+    sr = _host_shadow_rays(sc, rays, h, scenes.SPHERE_LIGHT)
+    t0 = time.perf_counter()
+    g.trace_any(sr, nthreads=nthreads)
+    t_shadow = time.perf_counter() - t0
+    n_prim = WIDTH * HEIGHT
+    n_shadow = sr.shape[0] * sample_stride
+    t_frame = t_build + (t_prim + t_shadow) * sample_stride
+    return dict(t_build=t_build, t_frame=t_frame, rays=n_prim + n_shadow, sampled=rays.shape[0] + sr.shape[0],
+                threads=pyoracle.max_threads() if nthreads <= 0 else nthreads)
+
+
+def _host_shadow_rays(sc, rays, h, light):
+    ok = h["id"] >= 0
+    tid = h["id"][ok]
+    v0 = sc.verts[sc.idx[tid, 0]].astype(np.float64)
+    e1 = sc.verts[sc.idx[tid, 1]] - v0
+    e2 = sc.verts[sc.idx[tid, 2]] - v0
+    n = np.cross(e1, e2)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    d = rays[ok, 4:7].astype(np.float64)
+    flip = (n * d).sum(1) > 0
+    n[flip] = -n[flip]
+    p = rays[ok, 0:3] + d * h["t"][ok, None] + n * 2e-4
+    L = light[None].astype(np.float64) - p
+    keep = (n * L).sum(1) > 0
+    sr = np.zeros((int(keep.sum()), 8), np.float32)
+    sr[:, 0:3] = p[keep]
+    sr[:, 3] = 2e-4
+    sr[:, 4:7] = L[keep]
+    sr[:, 7] = 1.0
+    return sr
+
+
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    k = 4
+    stride = 16
+    for w in range(args.warmup):
+        cpu_frame_sample(k, w % FRAMES, stride)
+    res = [cpu_frame_sample(k, s % FRAMES, stride) for s in range(args.steps)]
+    t = sum(r["t_frame"] for r in res)
+    rays = sum(r["rays"] for r in res)
+    value = rays / t / 1e6
+    cores = res[0]["threads"]
+    sample = (f"per frame: full single-thread grid build (k={k}) + every {stride}th primary ray and its shadow "
+              f"ray traced on {cores} threads, trace time x{stride}")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "k": k, "frames": FRAMES},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": sample, "build_ms": round(1e3 * statistics.median(r["t_build"] for r in res), 3)},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, ws, local, dist):
+    import torch
+    from gridrt import lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    v, idx, nrm = scenes.sphere_mesh()
+    nverts, ntris = v.shape[0], idx.shape[0]
+    cam = scenes.deforming_sphere_camera(WIDTH, HEIGHT)
+    npix = WIDTH * HEIGHT
+    light = scenes.SPHERE_LIGHT
+
+    s = lib.Scene(local)
+    s.set_geometry(v, idx)
+    stream = torch.cuda.ExternalStream(s.stream, device=dev)
+    d_base = torch.from_numpy(v).to(dev)
+    d_nrm = torch.from_numpy(nrm).to(dev)
+    d_hits = torch.empty((npix, 4), dtype=torch.int32, device=dev)
+    d_occ = torch.empty(npix, dtype=torch.uint8, device=dev)
+    d_sr = torch.empty((npix, 8), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    # capacities for every frame at every k (synchronous builds, untimed)
+    for k in LAMBDAS:
+        for f in range(FRAMES):
+            s.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+            s.build(k)
+
+    def frame(k, f, order, ev=None):
+        with torch.cuda.stream(stream):
+            if ev:
+                ev[0].record(stream)
+            s.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+            s.build_async(k)
+            if ev:
+                ev[1].record(stream)
+            s.trace_camera_device(cam, d_hits, light=light, d_shadow_rays=d_sr, order=order)
+            if ev:
+                ev[2].record(stream)
+            s.trace_any_device(d_sr, npix, d_occ)
+            if ev:
+                ev[3].record(stream)
+
+    # autotune the ray order once (k = 4, a few frames)
+    tune = {}
+    for order in ("scanline", "morton8"):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        for f in range(3):
+            frame(4, f, order)
+        frame(4, 3, order, evs)
+        torch.cuda.synchronize()
+        tune[order] = evs[1].elapsed_time(evs[3])
+    order = min(tune, key=tune.get)
+
+    per_k = {}
+    launches0 = lib.kernel_launches()
+    for k in LAMBDAS:
+        for w in range(args.warmup):
+            frame(k, w % FRAMES, order)
+        torch.cuda.synchronize()
+        if s.build_check() != 0:
+            raise RuntimeError("warm-up build failed: " + lib.load().rtg_last_error().decode())
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+        shadow_count = torch.zeros((), dtype=torch.int64, device=dev)
+        _barrier(dist)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if (k == LAMBDAS[1] and rank == 0) else None
+        if sampler:
+            sampler.__enter__()
+        lc0 = lib.kernel_launches()
+        for st in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()                      # L2 flush between frames (outside the events)
+            frame(k, st % FRAMES, order, evs[st])
+            with torch.cuda.stream(stream):
+                shadow_count += (d_sr[:, 7] >= 0).sum()
+        lc1 = lib.kernel_launches()
+        torch.cuda.synchronize()
+        _barrier(dist)
+        if sampler:
+            sampler.__exit__(None, None, None)
+        if s.build_check() != 0:
+            raise RuntimeError("timed build failed: " + lib.load().rtg_last_error().decode())
+        build_ms = [e[0].elapsed_time(e[1]) for e in evs]
+        prim_ms = [e[1].elapsed_time(e[2]) for e in evs]
+        shad_ms = [e[2].elapsed_time(e[3]) for e in evs]
+        frame_ms = [e[0].elapsed_time(e[3]) for e in evs]
+        total_s = _max_over_ranks(sum(frame_ms) / 1e3, dist)
+        rays = npix * args.steps + int(shadow_count.item())
+        rays_all = _sum_over_ranks(rays, dist)
+        per_k[k] = dict(value=rays_all / total_s / 1e6, ms_per_step=1e3 * total_s / args.steps,
+                        build_ms=statistics.median(build_ms), primary_ms=statistics.median(prim_ms),
+                        shadow_ms=statistics.median(shad_ms), rays_per_step=rays / args.steps,
+                        trace_mrays_s=rays / (sum(prim_ms) + sum(shad_ms)) / 1e3,
+                        launches=lc1 - lc0, clocks=sampler.summary() if sampler else None)
+
+    best_k = max(per_k, key=lambda kk: per_k[kk]["value"])
+    head = per_k[best_k]
+
+    # roofline of the dominant kernel (primary camera trace): algorithmic bytes
+    # from the traversal counters (16 B hit + 8 B per visited cell + 52 B per
+    # triangle test: 4 B list entry + 48 B record), camera rays read 0 B
+    s.deform(d_base, d_nrm, 0.05, 3.0, 0.0)
+    s.build(best_k)
+    s.counters(reset=True)
+    s.trace_camera_device(cam, d_hits, light=light, d_shadow_rays=d_sr, order=order, counters=True)
+    c = s.counters(reset=True)
+    alg_bytes = 16 * c["rays"] + 8 * c["cells"] + 52 * c["tests"]
+    # the kernel's own average duration (events around the launch alone)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    with torch.cuda.stream(stream):
+        ev0.record(stream)
+        for _ in range(reps):
+            s.trace_camera_device(cam, d_hits, light=light, d_shadow_rays=d_sr, order=order)
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    kern_s = ev0.elapsed_time(ev1) / 1e3 / reps
+    peak, peak_kind = _peaks()
+    achieved = alg_bytes / kern_s / 1e9
+    traffic = _traffic_from_profiles("trace_camera_kernel", alg_bytes)
+
+    # e2e through the public C ABI with host buffers
+    e2e = run_e2e(args, s, v, idx, nrm, cam, light, best_k, order, dist)
+
+    if rank != 0:
+        return
+    cpu = cpu_frame_sample(best_k, 0, 16)
+    clocks = per_k[LAMBDAS[1]]["clocks"] or {}
+    out = {
+        "metric": METRIC, "value": round(head["value"], 3), "unit": "Mrays/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "k": best_k, "ray_order": order, "frames": FRAMES, "triangles": ntris,
+                   "rays_primary": npix, "l2": "flushed between frames (256 MiB write, outside the timed events)",
+                   "parallelism": f"replicas x{ws}"},
+        "build_ms": round(head["build_ms"], 4), "trace_mrays_s": round(head["trace_mrays_s"], 2),
+        "per_k": {str(kk): {x: (round(y, 4) if isinstance(y, float) else y) for x, y in d.items() if x != "clocks"}
+                  for kk, d in per_k.items()},
+        "order_tune_ms": {o: round(t, 4) for o, t in tune.items()},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "trace_camera_kernel", "alg_bytes_per_launch": int(alg_bytes),
+                     "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"])},
+        "cpu_baseline": {"value": round(cpu["rays"] / cpu["t_frame"] / 1e6, 4), "unit": "Mrays/s",
+                         "cores": cpu["threads"], "kind": "port",
+                         "sample": f"frame 0, k={best_k}: single-thread grid build + every 16th primary ray and its "
+                                   f"shadow ray on {cpu['threads']} threads, trace time x16",
+                         "build_ms": round(cpu["t_build"] * 1e3, 3)},
+        "e2e": e2e,
+        "gpu_launches": int(head["launches"]),
+        "clocks": {"sm_mhz": clocks.get("sm_mhz"), "sm_max_mhz": clocks.get("sm_max_mhz"),
+                   "reasons": clocks.get("reasons", []), "samples": clocks.get("samples", 0)},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def _traffic_from_profiles(kernel: str, alg_bytes: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/traffic.json), or None."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(kernel, {}).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def run_e2e(args, s, v, idx, nrm, cam, light, k, order, dist):
+    import torch
+    from gridrt import lib
+    npix = cam.width * cam.height
+    host_verts = [torch.from_numpy(scenes.deform(v, nrm, f)).pin_memory() for f in range(FRAMES)]
+    hits = torch.empty((npix, 4), dtype=torch.int32).pin_memory()
+    occ = torch.empty(npix, dtype=torch.uint8).pin_memory()
+    nverts = v.shape[0]
+
+    def step(f):
+        s.update_vertices(host_verts[f], nverts, from_device=False)
+        s.build(k)
+        s.trace_frame(cam, light, hits, occ, order=order)
+
+    for w in range(args.warmup):
+        step(w % FRAMES)
+    _barrier(dist)
+    t0 = time.perf_counter()
+    shadow = 0
+    for st in range(args.steps):
+        step(st % FRAMES)
+        shadow += int((occ.numpy() != 2).sum())
+    t = _max_over_ranks(time.perf_counter() - t0, dist)
+    rays = _sum_over_ranks(npix * args.steps + shadow, dist)
+    return {"value": round(rays / t / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(nverts * 12),
+            "d2h_bytes_per_step": int(npix * 17), "ms_per_step": round(1e3 * t / args.steps, 3)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, ws, local, dist = _dist()
+    if args.impl == "reference":
+        run_reference(args, rank, ws, dist)
+    else:
+        run_gpu(args, rank, ws, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,706 @@
+// api.cu -- host side of the C ABI declared in include/gridrt.h.
+//
+// A scene owns its device buffers (geometry, triangle records, CSR grid,
+// build work areas, staging for host-pointer trace calls) and one stream.
+// Buffers grow on demand and are never shrunk; capacities carry 1/8 headroom
+// so per-frame rebuilds of a deforming mesh do not reallocate.
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/gridrt.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace gridrt;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+rtg_status fail(rtg_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define CUDA_TRY(expr)                                                                          \
+    do {                                                                                        \
+        cudaError_t _e = (expr);                                                                \
+        if (_e != cudaSuccess) {                                                                \
+            return fail(_e == cudaErrorMemoryAllocation ? RTG_NO_MEMORY : RTG_DEVICE_ERROR,     \
+                        std::string(#expr) + ": " + cudaGetErrorString(_e));                    \
+        }                                                                                       \
+    } while (0)
+
+template <class T>
+cudaError_t grow(T*& p, int64_t& cap, int64_t need) {
+    if (need <= cap && p) return cudaSuccess;
+    int64_t n = need + need / 8 + 64;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc((void**)&p, (size_t)n * sizeof(T));
+    if (e == cudaSuccess) cap = n;
+    return e;
+}
+
+}  // namespace
+
+struct rtg_scene_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+
+    float* d_verts = nullptr;
+    int64_t verts_cap = 0, nverts = 0;   // capacity in floats
+    int32_t* d_idx = nullptr;
+    int64_t idx_cap = 0, ntris = 0;      // capacity in ints
+    float4* d_tris = nullptr;
+    int64_t tris_cap = 0;                // float4 records
+
+    GridParams* d_params = nullptr;
+    GridParams* h_params = nullptr;      // pinned mirror
+    BuildWork* d_work = nullptr;
+    int32_t* d_offsets = nullptr;
+    int64_t cell_cap = 0;
+    int32_t* d_ids = nullptr;
+    int64_t ids_cap = 0;
+    int32_t* d_scratch = nullptr;
+    int64_t scratch_cap = 0;
+    int64_t* d_tiles = nullptr;
+    int64_t tiles_cap = 0;
+    int32_t* d_qs = nullptr;
+    int64_t qs_cap = 0;
+    int32_t* d_qm = nullptr;
+    int64_t qm_cap = 0;
+    int32_t* d_ql = nullptr;
+    int64_t ql_cap = 0;
+    int32_t bitmap_words = 32768;
+
+    bool built = false;
+    int32_t k = 0;
+    GridParams hp{};   // host copy of the last successful build
+
+    unsigned char* d_io = nullptr;
+    int64_t io_cap = 0;
+    TraceCounters* d_ctr = nullptr;
+};
+
+namespace {
+
+rtg_status set_device(rtg_scene s) {
+    CUDA_TRY(cudaSetDevice(s->device));
+    return RTG_OK;
+}
+
+int64_t ref_capacity(const rtg_scene s) { return s->ids_cap < s->scratch_cap ? s->ids_cap : s->scratch_cap; }
+
+rtg_status ensure_grid_buffers(rtg_scene s, int64_t cells_plus_one, int64_t refs) {
+    CUDA_TRY(grow(s->d_offsets, s->cell_cap, cells_plus_one));
+    CUDA_TRY(grow(s->d_tiles, s->tiles_cap, s->cell_cap / 4096 + 2));
+    CUDA_TRY(grow(s->d_ids, s->ids_cap, refs));
+    CUDA_TRY(grow(s->d_scratch, s->scratch_cap, refs));
+    const int64_t R = ref_capacity(s);
+    CUDA_TRY(grow(s->d_qs, s->qs_cap, R / 2 + 2));
+    CUDA_TRY(grow(s->d_qm, s->qm_cap, R / 33 + 2));
+    CUDA_TRY(grow(s->d_ql, s->ql_cap, R / 4097 + 2));
+    return RTG_OK;
+}
+
+BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
+    BuildArgs a;
+    a.verts = s->d_verts;
+    a.nverts = s->nverts;
+    a.idx = s->d_idx;
+    a.ntris = s->ntris;
+    a.k = k;
+    a.skip_bbox = skip_bbox;
+    a.params = s->d_params;
+    a.work = s->d_work;
+    a.tris = s->d_tris;
+    a.offsets = s->d_offsets;
+    a.cell_cap = s->cell_cap;
+    a.ids = s->d_ids;
+    a.scratch = s->d_scratch;
+    a.ref_cap = ref_capacity(s);
+    a.tile_sums = s->d_tiles;
+    a.q_small = s->d_qs;
+    a.q_med = s->d_qm;
+    a.q_large = s->d_ql;
+    a.q_small_cap = s->qs_cap;
+    a.q_med_cap = s->qm_cap;
+    a.q_large_cap = s->ql_cap;
+    a.bitmap_words = s->bitmap_words;
+    a.num_sms = s->num_sms;
+    return a;
+}
+
+// Host resolution of the grid parameters with the C library's powf, used when
+// the device flagged that the last ulp of powf decides a cell count.  Same
+// float operation order as src/rtplugins/UniformGridAccStructBuilder.cpp:86-98
+// and src/rtplugins/UniformGridAccStruct.cpp:56-62 (compiled without FMA
+// contraction).
+void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap) {
+    volatile float diag[3];
+    for (int d = 0; d < 3; ++d) diag[d] = p.bmax[d] - p.bmin[d];
+    volatile float v01 = diag[0] * diag[1];
+    volatile float V = v01 * diag[2];
+    const int32_t kn = (int32_t)((uint32_t)k * (uint32_t)ntris);
+    volatile float q = (float)kn / V;
+    volatile float factor = powf(q, 1.0f / 3.0f);
+    int64_t nc = 1;
+    uint32_t st = 0;
+    for (int d = 0; d < 3; ++d) {
+        volatile float m = diag[d] * factor;
+        float c = ceilf(m);
+        int32_t r = (c >= 1.0f && c < 2147483648.0f) ? (int32_t)c : 0;
+        if (r <= 0) st |= ST_TOO_BIG;
+        p.res[d] = r;
+        nc *= (r > 0 ? r : 1);
+    }
+    for (int d = 0; d < 3; ++d) {
+        volatile float ext = p.bmax[d] - p.bmin[d];
+        volatile float cs = ext / (float)(p.res[d] > 0 ? p.res[d] : 1);
+        p.cell[d] = cs;
+        p.inv[d] = 1.0f / cs;
+    }
+    if (nc >= INT32_MAX) st |= ST_TOO_BIG;
+    if (nc + 1 > cell_cap) st |= ST_CELL_CAP;
+    p.ncells = nc;
+    p.nrefs = 0;
+    p.k = k;
+    p.ntris = ntris;
+    p.status = st;
+}
+
+rtg_status read_params(rtg_scene s) {
+    CUDA_TRY(cudaMemcpyAsync(s->h_params, s->d_params, sizeof(GridParams), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return RTG_OK;
+}
+
+rtg_status read_clear_sticky(rtg_scene s, uint32_t* out) {
+    char* addr = reinterpret_cast<char*>(s->d_work) + offsetof(BuildWork, sticky);
+    CUDA_TRY(cudaMemcpyAsync(out, addr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemsetAsync(addr, 0, sizeof(uint32_t), s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return RTG_OK;
+}
+
+rtg_status enqueue_build(rtg_scene s, int32_t k, bool skip_bbox, cudaStream_t st) {
+    if (skip_bbox)
+        CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(s->d_work) + offsetof(BuildWork, nsort), 0,
+                                 sizeof(uint32_t) * 3, st));
+    launch_build(make_args(s, k, skip_bbox), st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status empty_grid(rtg_scene s, int32_t k) {
+    std::memset(&s->hp, 0, sizeof(GridParams));
+    s->hp.k = k;
+    s->built = true;
+    s->k = k;
+    return RTG_OK;
+}
+
+cudaStream_t pick(rtg_scene s, void* stream) { return stream ? (cudaStream_t)stream : s->stream; }
+
+SceneView view(rtg_scene s) {
+    SceneView v;
+    v.params = s->d_params;
+    v.offsets = s->d_offsets;
+    v.ids = s->d_ids;
+    v.tris = s->d_tris;
+    return v;
+}
+
+rtg_status ensure_io(rtg_scene s, int64_t bytes) {
+    if (bytes <= s->io_cap && s->d_io) return RTG_OK;
+    CUDA_TRY(grow(s->d_io, s->io_cap, bytes));
+    return RTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rtg_version(void) { return "gridrt 0.1 (sm_103a)"; }
+const char* rtg_last_error(void) { return g_last_error.c_str(); }
+
+rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
+    if (!out) return fail(RTG_INVALID_PARAM, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(RTG_INVALID_PARAM, "no such device");
+    CUDA_TRY(cudaSetDevice(device));
+    rtg_scene s = new rtg_scene_s();
+    s->device = device;
+    cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (stream) {
+        s->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete s;
+            return fail(RTG_DEVICE_ERROR, "stream creation failed");
+        }
+        s->own_stream = true;
+    }
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    // bitmap for the large-cell sort: up to 128 KiB (1M triangle ids per pass)
+    int words = 32768;
+    while (words * 4 + 4096 > max_optin && words > 1024) words >>= 1;
+    s->bitmap_words = words;
+    rtg_status rc = RTG_OK;
+    if (build_setup_attributes(words) != cudaSuccess) rc = fail(RTG_DEVICE_ERROR, "smem attribute");
+    if (rc == RTG_OK && cudaMalloc(&s->d_params, sizeof(GridParams)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "params");
+    if (rc == RTG_OK && cudaMallocHost(&s->h_params, sizeof(GridParams)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "pinned");
+    if (rc == RTG_OK && cudaMalloc(&s->d_work, sizeof(BuildWork)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "work");
+    if (rc == RTG_OK && cudaMalloc(&s->d_ctr, sizeof(TraceCounters)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "ctr");
+    if (rc == RTG_OK) {
+        BuildWork w;
+        std::memset(&w, 0, sizeof(w));
+        for (int d = 0; d < 3; ++d) { w.keys[d] = 0xffffffffu; w.keys[3 + d] = 0u; }
+        cudaMemcpy(s->d_work, &w, sizeof(w), cudaMemcpyHostToDevice);
+        cudaMemset(s->d_ctr, 0, sizeof(TraceCounters));
+        cudaMemset(s->d_params, 0, sizeof(GridParams));
+        if (cudaGetLastError() != cudaSuccess) rc = fail(RTG_DEVICE_ERROR, "init copies");
+    }
+    if (rc != RTG_OK) {
+        rtg_scene_destroy(s);
+        return rc;
+    }
+    *out = s;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_destroy(rtg_scene s) {
+    if (!s) return RTG_OK;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->d_verts);
+    cudaFree(s->d_idx);
+    cudaFree(s->d_tris);
+    cudaFree(s->d_params);
+    if (s->h_params) cudaFreeHost(s->h_params);
+    cudaFree(s->d_work);
+    cudaFree(s->d_offsets);
+    cudaFree(s->d_ids);
+    cudaFree(s->d_scratch);
+    cudaFree(s->d_tiles);
+    cudaFree(s->d_qs);
+    cudaFree(s->d_qm);
+    cudaFree(s->d_ql);
+    cudaFree(s->d_io);
+    cudaFree(s->d_ctr);
+    if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_stream(rtg_scene s, void** stream_out) {
+    if (!s || !stream_out) return fail(RTG_INVALID_PARAM, "NULL argument");
+    *stream_out = (void*)s->stream;
+    return RTG_OK;
+}
+
+static rtg_status set_geometry(rtg_scene s, const float* verts, int64_t nverts, const int32_t* tris, int64_t ntris,
+                               cudaMemcpyKind kind, cudaStream_t st) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (nverts < 0 || ntris < 0 || (nverts > 0 && !verts) || (ntris > 0 && !tris))
+        return fail(RTG_INVALID_PARAM, "bad geometry arrays");
+    if (ntris > (int64_t)INT32_MAX / 8 || nverts > (int64_t)INT32_MAX)
+        return fail(RTG_INVALID_PARAM, "geometry larger than the int32 index space");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    CUDA_TRY(grow(s->d_verts, s->verts_cap, 3 * nverts + 4));
+    CUDA_TRY(grow(s->d_idx, s->idx_cap, 3 * ntris + 4));
+    CUDA_TRY(grow(s->d_tris, s->tris_cap, 3 * ntris + 3));
+    if (nverts) CUDA_TRY(cudaMemcpyAsync(s->d_verts, verts, sizeof(float) * 3 * nverts, kind, st));
+    if (ntris) CUDA_TRY(cudaMemcpyAsync(s->d_idx, tris, sizeof(int32_t) * 3 * ntris, kind, st));
+    s->nverts = nverts;
+    s->ntris = ntris;
+    s->built = false;
+    if (st != s->stream) CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_set_geometry(rtg_scene s, const float* verts, int64_t nverts, const int32_t* tris, int64_t ntris,
+                                  void* stream) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    cudaStream_t st = pick(s, stream);
+    rtg_status rc = set_geometry(s, verts, nverts, tris, ntris, cudaMemcpyHostToDevice, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_set_geometry_device(rtg_scene s, const float* d_verts, int64_t nverts, const int32_t* d_tris,
+                                         int64_t ntris, void* stream) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    return set_geometry(s, d_verts, nverts, d_tris, ntris, cudaMemcpyDeviceToDevice, pick(s, stream));
+}
+
+rtg_status rtg_scene_update_vertices(rtg_scene s, const float* verts, int64_t nverts, int from_device, void* stream) {
+    if (!s || (!verts && nverts)) return fail(RTG_INVALID_PARAM, "NULL argument");
+    if (nverts != s->nverts) return fail(RTG_INVALID_PARAM, "vertex count differs from the scene's");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    cudaStream_t st = pick(s, stream);
+    if (nverts)
+        CUDA_TRY(cudaMemcpyAsync(s->d_verts, verts, sizeof(float) * 3 * nverts,
+                                 from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+    s->built = false;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_deform_vertices(rtg_scene s, const float* d_base, const float* d_normals, float amp, float freq,
+                                     float phase, void* stream) {
+    if (!s || !d_base || !d_normals) return fail(RTG_INVALID_PARAM, "NULL argument");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    launch_deform(d_base, d_normals, s->d_verts, s->nverts, amp, freq, phase, pick(s, stream));
+    CUDA_TRY(cudaGetLastError());
+    s->built = false;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_reserve(rtg_scene s, int64_t ncells, int64_t nrefs) {
+    if (!s || ncells < 0 || nrefs < 0) return fail(RTG_INVALID_PARAM, "bad reserve");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    return ensure_grid_buffers(s, ncells + 1, nrefs);
+}
+
+rtg_status rtg_scene_build_async(rtg_scene s, int32_t k, void* stream) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (k <= 0) return fail(RTG_INVALID_PARAM, "k must be positive");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    s->k = k;
+    if (s->ntris == 0 || s->nverts == 0) return empty_grid(s, k);
+    if (!s->d_offsets) {
+        rc = ensure_grid_buffers(s, 1, 1);
+        if (rc) return rc;
+    }
+    s->built = false;
+    return enqueue_build(s, k, false, pick(s, stream));
+}
+
+rtg_status rtg_scene_build_check(rtg_scene s, void* stream) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (s->ntris == 0 || s->nverts == 0) return s->built ? RTG_OK : fail(RTG_NOT_BUILT, "not built");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    CUDA_TRY(cudaStreamSynchronize(pick(s, stream)));
+    rc = read_params(s);
+    if (rc) return rc;
+    uint32_t sticky = 0;
+    rc = read_clear_sticky(s, &sticky);
+    if (rc) return rc;
+    const uint32_t st = s->h_params->status | sticky;
+    if (st & (ST_CELL_CAP | ST_REF_CAP | ST_SORT_CAP | ST_AMBIGUOUS))
+        return fail(RTG_NO_MEMORY, "asynchronous build needs a synchronous rebuild (capacity or resolution)");
+    if (st & ST_TOO_BIG) return fail(RTG_INVALID_PARAM, "grid exceeds the int32 index space");
+    if (st & ST_BAD_RANGE) return fail(RTG_INVALID_GEOMETRY, "non-finite vertex or triangle outside the grid");
+    s->hp = *s->h_params;
+    s->built = true;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_build(rtg_scene s, int32_t k, void* stream) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (k <= 0) return fail(RTG_INVALID_PARAM, "k must be positive");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    cudaStream_t st = pick(s, stream);
+    if (st != s->stream) {
+        // keep the scene's own stream ordered behind the caller's
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    s->k = k;
+    if (s->ntris == 0 || s->nverts == 0) return empty_grid(s, k);
+    if (!s->d_offsets) {
+        rc = ensure_grid_buffers(s, 1, 1);
+        if (rc) return rc;
+    }
+    s->built = false;
+    bool skip_bbox = false;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        rc = enqueue_build(s, k, skip_bbox, s->stream);
+        if (rc) return rc;
+        rc = read_params(s);
+        if (rc) return rc;
+        GridParams p = *s->h_params;
+        if (p.status & ST_TOO_BIG) return fail(RTG_INVALID_PARAM, "grid exceeds the int32 index space");
+        if (p.status & ST_AMBIGUOUS) {
+            host_resolve(p, k, s->ntris, s->cell_cap);
+            if (p.status & ST_TOO_BIG) return fail(RTG_INVALID_PARAM, "grid exceeds the int32 index space");
+            if (p.status & ST_CELL_CAP) {
+                rc = ensure_grid_buffers(s, p.ncells + 1, ref_capacity(s));
+                if (rc) return rc;
+                p.status &= ~ST_CELL_CAP;
+            }
+            CUDA_TRY(cudaMemcpyAsync(s->d_params, &p, sizeof(GridParams), cudaMemcpyHostToDevice, s->stream));
+            skip_bbox = true;
+            continue;
+        }
+        if (p.status & ST_CELL_CAP) {
+            const int64_t guess = ref_capacity(s) > 8 * s->ntris ? ref_capacity(s) : 8 * s->ntris;
+            rc = ensure_grid_buffers(s, p.ncells + 1, guess);
+            if (rc) return rc;
+            skip_bbox = false;
+            continue;
+        }
+        if (p.status & (ST_REF_CAP | ST_SORT_CAP)) {
+            rc = ensure_grid_buffers(s, s->cell_cap, p.nrefs);
+            if (rc) return rc;
+            skip_bbox = false;
+            continue;
+        }
+        if (p.status & ST_BAD_RANGE)
+            return fail(RTG_INVALID_GEOMETRY, "non-finite vertex or triangle outside the grid");
+        s->hp = p;
+        s->built = true;
+        uint32_t sticky = 0;
+        return read_clear_sticky(s, &sticky);   // earlier attempts of this call are resolved
+    }
+    return fail(RTG_DEVICE_ERROR, "grid build did not converge");
+}
+
+rtg_status rtg_scene_grid_info(rtg_scene s, rtg_grid_info* out) {
+    if (!s || !out) return fail(RTG_INVALID_PARAM, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    const GridParams& p = s->hp;
+    for (int d = 0; d < 3; ++d) {
+        out->res[d] = p.res[d];
+        out->bmin[d] = p.bmin[d];
+        out->bmax[d] = p.bmax[d];
+        out->cell[d] = p.cell[d];
+        out->inv_cell[d] = p.inv[d];
+    }
+    out->ncells = p.ncells;
+    out->nrefs = p.nrefs;
+    out->k = s->k;
+    out->built = s->built ? 1 : 0;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_grid_download(rtg_scene s, int32_t* offsets, int32_t* ids) {
+    if (!s || !offsets) return fail(RTG_INVALID_PARAM, "NULL argument");
+    if (!s->built) return fail(RTG_NOT_BUILT, "scene not built");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    if (s->hp.ncells == 0) {
+        offsets[0] = 0;
+        return RTG_OK;
+    }
+    CUDA_TRY(cudaMemcpyAsync(offsets, s->d_offsets, sizeof(int32_t) * (s->hp.ncells + 1), cudaMemcpyDeviceToHost,
+                             s->stream));
+    if (s->hp.nrefs && ids)
+        CUDA_TRY(cudaMemcpyAsync(ids, s->d_ids, sizeof(int32_t) * s->hp.nrefs, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_download_vertices(rtg_scene s, float* verts) {
+    if (!s || (!verts && s->nverts)) return fail(RTG_INVALID_PARAM, "NULL argument");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    if (s->nverts)
+        CUDA_TRY(cudaMemcpyAsync(verts, s->d_verts, sizeof(float) * 3 * s->nverts, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_grid_device(rtg_scene s, const int32_t** d_offsets, const int32_t** d_ids, const float** d_tris) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (d_offsets) *d_offsets = s->d_offsets;
+    if (d_ids) *d_ids = s->d_ids;
+    if (d_tris) *d_tris = reinterpret_cast<const float*>(s->d_tris);
+    return RTG_OK;
+}
+
+static rtg_status check_traceable(rtg_scene s, int64_t n) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (n < 0) return fail(RTG_INVALID_PARAM, "negative ray count");
+    if (!s->built) return fail(RTG_NOT_BUILT, "scene not built");
+    return set_device(s);
+}
+
+rtg_status rtg_trace_nearest_device(rtg_scene s, const float* d_rays, int64_t n, rtg_hit* d_hits, int32_t flags,
+                                    void* stream) {
+    rtg_status rc = check_traceable(s, n);
+    if (rc) return rc;
+    if (n == 0) return RTG_OK;
+    if (!d_rays || !d_hits) return fail(RTG_INVALID_PARAM, "NULL arrays");
+    cudaStream_t st = pick(s, stream);
+    if (s->hp.ncells == 0) {
+        CUDA_TRY(cudaMemsetAsync(d_hits, 0xff, sizeof(rtg_hit) * n, st));   // id = -1 (t/u/v NaN-bit pattern)
+        return RTG_OK;
+    }
+    launch_trace_nearest(view(s), reinterpret_cast<const float4*>(d_rays), n, reinterpret_cast<int4*>(d_hits),
+                         (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, s->num_sms, st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_any_device(rtg_scene s, const float* d_rays, int64_t n, uint8_t* d_occ, int32_t flags,
+                                void* stream) {
+    rtg_status rc = check_traceable(s, n);
+    if (rc) return rc;
+    if (n == 0) return RTG_OK;
+    if (!d_rays || !d_occ) return fail(RTG_INVALID_PARAM, "NULL arrays");
+    cudaStream_t st = pick(s, stream);
+    if (s->hp.ncells == 0) {
+        CUDA_TRY(cudaMemsetAsync(d_occ, 0, n, st));
+        return RTG_OK;
+    }
+    launch_trace_any(view(s), reinterpret_cast<const float4*>(d_rays), n, d_occ,
+                     (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, s->num_sms, st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_nearest(rtg_scene s, const float* rays, int64_t n, rtg_hit* hits, int32_t flags, void* stream) {
+    rtg_status rc = check_traceable(s, n);
+    if (rc) return rc;
+    if (n == 0) return RTG_OK;
+    if (!rays || !hits) return fail(RTG_INVALID_PARAM, "NULL arrays");
+    cudaStream_t st = pick(s, stream);
+    rc = ensure_io(s, n * 48);
+    if (rc) return rc;
+    float* d_rays = reinterpret_cast<float*>(s->d_io);
+    rtg_hit* d_hits = reinterpret_cast<rtg_hit*>(s->d_io + n * 32);
+    CUDA_TRY(cudaMemcpyAsync(d_rays, rays, n * 32, cudaMemcpyHostToDevice, st));
+    rc = rtg_trace_nearest_device(s, d_rays, n, d_hits, flags, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(hits, d_hits, n * 16, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_any(rtg_scene s, const float* rays, int64_t n, uint8_t* occ, int32_t flags, void* stream) {
+    rtg_status rc = check_traceable(s, n);
+    if (rc) return rc;
+    if (n == 0) return RTG_OK;
+    if (!rays || !occ) return fail(RTG_INVALID_PARAM, "NULL arrays");
+    cudaStream_t st = pick(s, stream);
+    rc = ensure_io(s, n * 33 + 16);
+    if (rc) return rc;
+    float* d_rays = reinterpret_cast<float*>(s->d_io);
+    uint8_t* d_occ = s->d_io + n * 32;
+    CUDA_TRY(cudaMemcpyAsync(d_rays, rays, n * 32, cudaMemcpyHostToDevice, st));
+    rc = rtg_trace_any_device(s, d_rays, n, d_occ, flags, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(occ, d_occ, n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+static bool camera_ok(const rtg_camera* cam) {
+    if (!cam || cam->width <= 0 || cam->height <= 0) return false;
+    if ((int64_t)cam->width * cam->height > ((int64_t)1 << 31)) return false;
+    if (cam->order == RTG_ORDER_MORTON8 && ((cam->width & 7) || (cam->height & 7))) return false;
+    return cam->order == RTG_ORDER_SCANLINE || cam->order == RTG_ORDER_MORTON8;
+}
+
+static CameraArgs camera_args(const rtg_camera* cam) {
+    CameraArgs c;
+    for (int a = 0; a < 3; ++a) {
+        c.eye[a] = cam->eye[a];
+        c.base[a] = cam->base_dir[a];
+        c.nu[a] = cam->near_u[a];
+        c.nv[a] = cam->near_v[a];
+    }
+    // PinholeCamera::newFrame: _invWidth = 1.0f / _screenWidth (src/rtplugins/PinholeCamera.cpp:52-53)
+    volatile float w = (float)cam->width, h = (float)cam->height;
+    c.inv_w = 1.0f / w;
+    c.inv_h = 1.0f / h;
+    c.width = cam->width;
+    c.height = cam->height;
+    c.order = cam->order;
+    return c;
+}
+
+rtg_status rtg_trace_camera_device(rtg_scene s, const rtg_camera* cam, rtg_hit* d_hits, const float* light_pos,
+                                   float* d_shadow_rays, int32_t flags, void* stream) {
+    rtg_status rc = check_traceable(s, 0);
+    if (rc) return rc;
+    if (!camera_ok(cam)) return fail(RTG_INVALID_PARAM, "bad camera (size, or Morton order needs multiples of 8)");
+    if (!d_hits) return fail(RTG_INVALID_PARAM, "NULL hits");
+    cudaStream_t st = pick(s, stream);
+    const int64_t n = (int64_t)cam->width * cam->height;
+    if (s->hp.ncells == 0) {
+        CUDA_TRY(cudaMemsetAsync(d_hits, 0xff, sizeof(rtg_hit) * n, st));
+        if (d_shadow_rays) CUDA_TRY(cudaMemsetAsync(d_shadow_rays, 0xff, 32 * n, st));
+        return RTG_OK;
+    }
+    launch_trace_camera(view(s), camera_args(cam), reinterpret_cast<int4*>(d_hits), light_pos,
+                        reinterpret_cast<float4*>(d_shadow_rays), (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr,
+                        s->num_sms, st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_frame_device(rtg_scene s, const rtg_camera* cam, const float* light_pos, rtg_hit* d_hits,
+                                  uint8_t* d_occ, float* d_shadow_rays, void* stream) {
+    if (!light_pos || !d_occ || !d_shadow_rays) return fail(RTG_INVALID_PARAM, "NULL arguments");
+    rtg_status rc = rtg_trace_camera_device(s, cam, d_hits, light_pos, d_shadow_rays, 0, stream);
+    if (rc) return rc;
+    const int64_t n = (int64_t)cam->width * cam->height;
+    cudaStream_t st = pick(s, stream);
+    if (s->hp.ncells == 0) {
+        CUDA_TRY(cudaMemsetAsync(d_occ, 2, n, st));
+        return RTG_OK;
+    }
+    launch_trace_any(view(s), reinterpret_cast<const float4*>(d_shadow_rays), n, d_occ, nullptr, s->num_sms, st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_frame(rtg_scene s, const rtg_camera* cam, const float* light_pos, rtg_hit* hits,
+                           uint8_t* occluded, void* stream) {
+    rtg_status rc = check_traceable(s, 0);
+    if (rc) return rc;
+    if (!camera_ok(cam)) return fail(RTG_INVALID_PARAM, "bad camera");
+    if (!light_pos || !hits || !occluded) return fail(RTG_INVALID_PARAM, "NULL arguments");
+    const int64_t n = (int64_t)cam->width * cam->height;
+    rc = ensure_io(s, n * (16 + 32 + 1) + 64);
+    if (rc) return rc;
+    rtg_hit* d_hits = reinterpret_cast<rtg_hit*>(s->d_io);
+    float* d_sr = reinterpret_cast<float*>(s->d_io + n * 16);
+    uint8_t* d_occ = s->d_io + n * 48;
+    cudaStream_t st = pick(s, stream);
+    rc = rtg_trace_frame_device(s, cam, light_pos, d_hits, d_occ, d_sr, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(hits, d_hits, n * 16, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(occluded, d_occ, n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+uint64_t rtg_kernel_launch_count(void) { return (uint64_t)launches_so_far(); }
+
+rtg_status rtg_scene_counters(rtg_scene s, int64_t out[3], int reset) {
+    if (!s || !out) return fail(RTG_INVALID_PARAM, "NULL argument");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    TraceCounters c;
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaMemcpy(&c, s->d_ctr, sizeof(c), cudaMemcpyDeviceToHost));
+    out[0] = (int64_t)c.rays;
+    out[1] = (int64_t)c.cells;
+    out[2] = (int64_t)c.tests;
+    if (reset) CUDA_TRY(cudaMemset(s->d_ctr, 0, sizeof(c)));
+    return RTG_OK;
+}
+
+}  // extern "C"

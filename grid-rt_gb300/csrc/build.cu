@@ -1,0 +1,690 @@
+// build.cu -- per-frame uniform-grid construction on the device.
+//
+// Replaces rtp::UniformGridAccStructBuilder::buildUniformGrid
+// (src/rtplugins/UniformGridAccStructBuilder.cpp:71-149) and the GPU grid
+// passes the reference drove through GLSL (shaders/countCellFP.glsl:39-73,
+// gridAccumVP_sem_GS.glsl:27-38, gridFP.glsl:60-131).  Output is a CSR grid:
+// offsets[ncells + 1] and ids[nrefs], each cell's list sorted by triangle id,
+// bit-identical to the reference's per-cell std::vector lists.
+//
+// Pipeline (all on one stream, no host round trip):
+//   bbox_params   scene box (exact min/max), 1% enlargement, resolution rule;
+//                 the last block derives the grid parameters on the device
+//   zero_offsets  clears offsets[0..ncells]
+//   count         warp-cooperative expansion of each triangle's cell range;
+//                 warp-aggregated atomicAdd of per-cell counts; writes the
+//                 Moller-Trumbore triangle records {v0|id, e1, e2}
+//   scan x3       in-place inclusive scan of the counts (cursors = cell ends)
+//   scatter       same expansion; warp-aggregated atomicSub on the cursors,
+//                 which leaves them equal to the exclusive cell starts
+//   sort x3       per-cell sort by triangle id: warp bitonic (<= 32), block
+//                 bitonic in shared memory (<= 4096), shared-memory bitmap
+//                 compaction for larger cells (ids within a cell are unique)
+#include "common.cuh"
+#include "kernels.h"
+
+#include <climits>
+
+namespace gridrt {
+
+static constexpr unsigned FULL = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// bbox + grid parameters
+// ---------------------------------------------------------------------------
+// Aabb::buildFrom / expandBy (src/rtcore/Aabb.cpp:11-53): min/max per axis.
+// A NaN coordinate never wins a comparison there, so it is skipped here too.
+__global__ void __launch_bounds__(256) bbox_params_kernel(const float* __restrict__ verts, int64_t nverts,
+                                                          BuildWork* w, GridParams* p, int32_t k, int64_t ntris,
+                                                          int64_t cell_cap) {
+    float mn0 = INFINITY, mn1 = INFINITY, mn2 = INFINITY;
+    float mx0 = -INFINITY, mx1 = -INFINITY, mx2 = -INFINITY;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nverts; i += stride) {
+        const float a = __ldg(verts + 3 * i), b = __ldg(verts + 3 * i + 1), c = __ldg(verts + 3 * i + 2);
+        mn0 = a < mn0 ? a : mn0; mx0 = a > mx0 ? a : mx0;
+        mn1 = b < mn1 ? b : mn1; mx1 = b > mx1 ? b : mx1;
+        mn2 = c < mn2 ? c : mn2; mx2 = c > mx2 ? c : mx2;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        float t;
+        t = __shfl_xor_sync(FULL, mn0, o); mn0 = t < mn0 ? t : mn0;
+        t = __shfl_xor_sync(FULL, mn1, o); mn1 = t < mn1 ? t : mn1;
+        t = __shfl_xor_sync(FULL, mn2, o); mn2 = t < mn2 ? t : mn2;
+        t = __shfl_xor_sync(FULL, mx0, o); mx0 = t > mx0 ? t : mx0;
+        t = __shfl_xor_sync(FULL, mx1, o); mx1 = t > mx1 ? t : mx1;
+        t = __shfl_xor_sync(FULL, mx2, o); mx2 = t > mx2 ? t : mx2;
+    }
+    __shared__ float red[6][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][wid] = mn0; red[1][wid] = mn1; red[2][wid] = mn2;
+        red[3][wid] = mx0; red[4][wid] = mx1; red[5][wid] = mx2;
+    }
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int i = 1; i < nw; ++i) {
+            mn0 = red[0][i] < mn0 ? red[0][i] : mn0;
+            mn1 = red[1][i] < mn1 ? red[1][i] : mn1;
+            mn2 = red[2][i] < mn2 ? red[2][i] : mn2;
+            mx0 = red[3][i] > mx0 ? red[3][i] : mx0;
+            mx1 = red[4][i] > mx1 ? red[4][i] : mx1;
+            mx2 = red[5][i] > mx2 ? red[5][i] : mx2;
+        }
+        atomicMin(&w->keys[0], f2key(mn0));
+        atomicMin(&w->keys[1], f2key(mn1));
+        atomicMin(&w->keys[2], f2key(mn2));
+        atomicMax(&w->keys[3], f2key(mx0));
+        atomicMax(&w->keys[4], f2key(mx1));
+        atomicMax(&w->keys[5], f2key(mx2));
+        __threadfence();
+        const uint32_t ticket = atomicAdd(&w->ticket, 1u);
+        last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+
+    // ---- last block: grid parameters --------------------------------------
+    float mn[3], mx[3];
+    for (int d = 0; d < 3; ++d) {
+        mn[d] = key2f(atomicAdd(&w->keys[d], 0u));
+        mx[d] = key2f(atomicAdd(&w->keys[3 + d], 0u));
+        w->keys[d] = 0xffffffffu;   // reset for the next build
+        w->keys[3 + d] = 0u;
+    }
+    w->ticket = 0u;
+    w->nsort[0] = w->nsort[1] = w->nsort[2] = 0u;
+    // Aabb::scaleBy(0.01f) with planar tolerance 0.01f (src/rtcore/Aabb.cpp:78-91)
+    for (int d = 0; d < 3; ++d) {
+        const float s = (mn[d] == mx[d]) ? 0.01f : fmul(vabs(fsub(mx[d], mn[d])), 0.01f);
+        mn[d] = fsub(mn[d], s);
+        mx[d] = fadd(mx[d], s);
+    }
+    // src/rtplugins/UniformGridAccStructBuilder.cpp:86-98
+    float diag[3];
+    for (int d = 0; d < 3; ++d) diag[d] = fsub(mx[d], mn[d]);
+    const float V = fmul(fmul(diag[0], diag[1]), diag[2]);
+    const int32_t kn = (int32_t)((uint32_t)k * (uint32_t)ntris);
+    const float q = fdiv(__int2float_rn(kn), V);
+    // powf(q, 1/3): the device evaluates pow in double and rounds to float;
+    // the host's powf may differ from that by one ulp, so the resolution is
+    // accepted only when ceil(d*f) is the same for f-1ulp, f, f+1ulp.
+    const float f = __double2float_rn(pow((double)q, (double)(1.0f / 3.0f)));
+    const float fm = nextafterf(f, 0.0f), fp = nextafterf(f, INFINITY);
+    uint32_t status = 0;
+    int64_t ncells = 1;
+    for (int d = 0; d < 3; ++d) {
+        const float a = ceilf(fmul(diag[d], fm));
+        const float b = ceilf(fmul(diag[d], f));
+        const float c = ceilf(fmul(diag[d], fp));
+        if (a != c) status |= ST_AMBIGUOUS;
+        int32_t r = (b >= 1.0f && b < 2147483648.0f) ? (int32_t)b : 0;
+        if (r <= 0) status |= ST_TOO_BIG;
+        p->res[d] = r;
+        ncells *= (r > 0 ? r : 1);
+    }
+    for (int d = 0; d < 3; ++d) {
+        p->bmin[d] = mn[d];
+        p->bmax[d] = mx[d];
+        const float cs = fdiv(fsub(mx[d], mn[d]), __int2float_rn(p->res[d] > 0 ? p->res[d] : 1));
+        p->cell[d] = cs;
+        p->inv[d] = frcp(cs);
+    }
+    if (ncells >= INT32_MAX) status |= ST_TOO_BIG;
+    if (ncells + 1 > cell_cap) status |= ST_CELL_CAP;
+    p->k = k;
+    p->ncells = ncells;
+    p->nrefs = 0;
+    p->ntris = ntris;
+    p->status = status;
+    if (status) atomicOr(&w->sticky, status);
+}
+
+static __device__ __forceinline__ bool fatal(uint32_t s) {
+    return (s & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG)) != 0;
+}
+
+__global__ void zero_offsets_kernel(int32_t* __restrict__ offsets, const GridParams* __restrict__ p) {
+    if (fatal(p->status)) return;
+    const int64_t n = p->ncells + 1;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {
+        if (i + 4 <= n && ((i & 3) == 0)) {
+            reinterpret_cast<int4*>(offsets)[i >> 2] = make_int4(0, 0, 0, 0);
+        } else {
+            for (int64_t j = i; j < n && j < i + 4; ++j) offsets[j] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-triangle cell ranges, expanded cooperatively by a warp
+// ---------------------------------------------------------------------------
+struct Lite {
+    float bmin[3], inv[3];
+    int32_t res[3];
+};
+
+__device__ __forceinline__ void load_lite(const GridParams* p, Lite& L) {
+    for (int d = 0; d < 3; ++d) {
+        L.bmin[d] = p->bmin[d];
+        L.inv[d] = p->inv[d];
+        L.res[d] = p->res[d];
+    }
+}
+
+// Triangle box (v0, then expandBy v1, v2 with the reference's if / else-if)
+// and its cell range, src/rtplugins/UniformGridAccStructBuilder.cpp:111-127.
+__device__ __forceinline__ void tri_box_range(const Lite& L, const float3& v0, const float3& v1, const float3& v2,
+                                              int32_t lo[3], int32_t hi[3]) {
+    float bmn[3] = {v0.x, v0.y, v0.z}, bmx[3] = {v0.x, v0.y, v0.z};
+    const float a1[3] = {v1.x, v1.y, v1.z}, a2[3] = {v2.x, v2.y, v2.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (a1[d] < bmn[d]) bmn[d] = a1[d];
+        else if (a1[d] > bmx[d]) bmx[d] = a1[d];
+        if (a2[d] < bmn[d]) bmn[d] = a2[d];
+        else if (a2[d] > bmx[d]) bmx[d] = a2[d];
+        lo[d] = world_to_voxel(bmn[d], L.bmin[d], L.inv[d]);
+        hi[d] = world_to_voxel(bmx[d], L.bmin[d], L.inv[d]);
+    }
+}
+
+__device__ __forceinline__ float3 load_vert(const float* __restrict__ verts, int32_t v) {
+    const float* q = verts + 3 * (int64_t)v;
+    return make_float3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
+}
+
+// Enumerates every (cell, triangle) reference of the warp's 32 triangles, 32
+// references per step, and calls emit(cell, tri, active) on every lane.
+template <bool WRITE_TRIS, class Emit>
+__device__ __forceinline__ void warp_expand(const Lite& L, const float* __restrict__ verts,
+                                            const int32_t* __restrict__ idx, int64_t ntris, int64_t base,
+                                            float4* __restrict__ tris, GridParams* p, BuildWork* w,
+                                            Emit&& emit) {
+    const int lane = threadIdx.x & 31;
+    const int64_t t = base + lane;
+    int32_t lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
+    uint32_t cnt = 0;
+    if (t < ntris) {
+        const int32_t i0 = __ldg(idx + 3 * t), i1 = __ldg(idx + 3 * t + 1), i2 = __ldg(idx + 3 * t + 2);
+        const float3 v0 = load_vert(verts, i0), v1 = load_vert(verts, i1), v2 = load_vert(verts, i2);
+        int32_t hi[3];
+        tri_box_range(L, v0, v1, v2, lo, hi);
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            ok = ok && lo[d] >= 0 && hi[d] < L.res[d] && lo[d] <= hi[d];
+            ext[d] = hi[d] - lo[d] + 1;
+        }
+        if (ok) {
+            cnt = (uint32_t)ext[0] * (uint32_t)ext[1] * (uint32_t)ext[2];
+        } else {
+            raise_status(p, w, ST_BAD_RANGE);
+            ext[0] = ext[1] = ext[2] = 1;
+        }
+        if (WRITE_TRIS) {
+            tris[3 * t + 0] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int32_t)t));
+            tris[3 * t + 1] = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.0f);
+            tris[3 * t + 2] = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.0f);
+        }
+    }
+    unsigned long long incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const unsigned long long total = __shfl_sync(FULL, incl, 31);
+    const unsigned long long excl = incl - cnt;
+    for (unsigned long long r0 = 0; r0 < total; r0 += 32) {
+        const unsigned long long r = r0 + lane;
+        const bool active = r < total;
+        // owner lane j: smallest j with incl_j > r (exactly 5 halvings)
+        int lo_ = 0, hi_ = 31;
+#pragma unroll
+        for (int s = 0; s < 5; ++s) {
+            const int mid = (lo_ + hi_) >> 1;
+            const unsigned long long im = __shfl_sync(FULL, incl, mid);
+            if (im > r) hi_ = mid; else lo_ = mid + 1;
+        }
+        const int j = lo_;
+        const unsigned long long ex_j = __shfl_sync(FULL, excl, j);
+        const int32_t lx = __shfl_sync(FULL, lo[0], j), ly = __shfl_sync(FULL, lo[1], j),
+                      lz = __shfl_sync(FULL, lo[2], j);
+        const int32_t ex = __shfl_sync(FULL, ext[0], j), ey = __shfl_sync(FULL, ext[1], j);
+        const uint32_t l = (uint32_t)(r - ex_j);
+        const uint32_t rest = l / (uint32_t)ex;
+        const int32_t x = lx + (int32_t)(l - rest * (uint32_t)ex);
+        const int32_t y = ly + (int32_t)(rest % (uint32_t)ey);
+        const int32_t z = lz + (int32_t)(rest / (uint32_t)ey);
+        const int32_t cell = active ? (x + y * L.res[0] + z * L.res[0] * L.res[1]) : -1;
+        emit(cell, (int32_t)(base + j), active);
+    }
+    if (lane == 0 && total) atomicAdd(reinterpret_cast<unsigned long long*>(&p->nrefs), total);
+}
+
+__global__ void __launch_bounds__(256) count_kernel(const float* __restrict__ verts, const int32_t* __restrict__ idx,
+                                                    int64_t ntris, GridParams* p, BuildWork* w,
+                                                    int32_t* __restrict__ counts, float4* __restrict__ tris) {
+    if (fatal(p->status)) return;
+    Lite L;
+    load_lite(p, L);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
+        warp_expand<true>(L, verts, idx, ntris, base, tris, p, w, [&](int32_t cell, int32_t, bool active) {
+            const unsigned peers = __match_any_sync(FULL, cell);
+            const int leader = __ffs(peers) - 1;
+            if (active && lane == leader) atomicAdd(&counts[cell], __popc(peers));
+        });
+    }
+}
+
+__global__ void __launch_bounds__(256) scatter_kernel(const float* __restrict__ verts, const int32_t* __restrict__ idx,
+                                                      int64_t ntris, GridParams* p, int32_t* __restrict__ cursor,
+                                                      int32_t* __restrict__ ids) {
+    if (p->status & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP)) return;
+    Lite L;
+    load_lite(p, L);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
+        const int64_t t = base + lane;
+        int32_t lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
+        uint32_t cnt = 0;
+        if (t < ntris) {
+            const int32_t i0 = __ldg(idx + 3 * t), i1 = __ldg(idx + 3 * t + 1), i2 = __ldg(idx + 3 * t + 2);
+            const float3 v0 = load_vert(verts, i0), v1 = load_vert(verts, i1), v2 = load_vert(verts, i2);
+            int32_t hi[3];
+            tri_box_range(L, v0, v1, v2, lo, hi);
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                ok = ok && lo[d] >= 0 && hi[d] < L.res[d] && lo[d] <= hi[d];
+                ext[d] = hi[d] - lo[d] + 1;
+            }
+            if (ok) cnt = (uint32_t)ext[0] * (uint32_t)ext[1] * (uint32_t)ext[2];
+            else ext[0] = ext[1] = ext[2] = 1;
+        }
+        unsigned long long incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const unsigned long long total = __shfl_sync(FULL, incl, 31);
+        const unsigned long long excl = incl - cnt;
+        for (unsigned long long r0 = 0; r0 < total; r0 += 32) {
+            const unsigned long long r = r0 + lane;
+            const bool active = r < total;
+            int lo_ = 0, hi_ = 31;
+#pragma unroll
+            for (int s = 0; s < 5; ++s) {
+                const int mid = (lo_ + hi_) >> 1;
+                const unsigned long long im = __shfl_sync(FULL, incl, mid);
+                if (im > r) hi_ = mid; else lo_ = mid + 1;
+            }
+            const int j = lo_;
+            const unsigned long long ex_j = __shfl_sync(FULL, excl, j);
+            const int32_t lx = __shfl_sync(FULL, lo[0], j), ly = __shfl_sync(FULL, lo[1], j),
+                          lz = __shfl_sync(FULL, lo[2], j);
+            const int32_t ex = __shfl_sync(FULL, ext[0], j), ey = __shfl_sync(FULL, ext[1], j);
+            const uint32_t l = (uint32_t)(r - ex_j);
+            const uint32_t rest = l / (uint32_t)ex;
+            const int32_t x = lx + (int32_t)(l - rest * (uint32_t)ex);
+            const int32_t y = ly + (int32_t)(rest % (uint32_t)ey);
+            const int32_t z = lz + (int32_t)(rest / (uint32_t)ey);
+            const int32_t cell = active ? (x + y * L.res[0] + z * L.res[0] * L.res[1]) : -1;
+            const unsigned peers = __match_any_sync(FULL, cell);
+            const int leader = __ffs(peers) - 1;
+            const int g = __popc(peers);
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            int32_t old = 0;
+            if (active && lane == leader) old = atomicSub(&cursor[cell], g);
+            old = __shfl_sync(FULL, old, leader);
+            if (active) ids[old - g + rank] = (int32_t)(base + j);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// scan of the per-cell counts (in place, inclusive), three phases
+// ---------------------------------------------------------------------------
+static constexpr int SCAN_THREADS = 256;
+static constexpr int SCAN_ITEMS = 16;
+static constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;   // 4096 cells
+
+__device__ __forceinline__ int64_t block_sum_i64(int64_t v, int64_t* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    int64_t s = 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+        sh[32] = s;
+    }
+    __syncthreads();
+    s = sh[32];
+    __syncthreads();
+    return s;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const int32_t* __restrict__ counts,
+                                                                   const GridParams* __restrict__ p,
+                                                                   int64_t* __restrict__ tile_sums) {
+    if (fatal(p->status)) return;
+    const int64_t C = p->ncells;
+    const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
+    __shared__ int64_t sh[33];
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t b = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+        int64_t s = 0;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; ++i)
+            if (b + i < C) s += counts[b + i];
+        s = block_sum_i64(s, sh);
+        if (threadIdx.x == 0) tile_sums[tile] = s;
+    }
+}
+
+__global__ void __launch_bounds__(1024) scan_tiles_kernel(GridParams* p, BuildWork* w, int64_t* __restrict__ tile_sums,
+                                                          int32_t* __restrict__ offsets, int64_t ref_cap) {
+    if (fatal(p->status)) return;
+    const int64_t C = p->ncells;
+    const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
+    __shared__ int64_t sh[33];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t b = 0; b < ntiles; b += blockDim.x) {
+        const int64_t i = b + threadIdx.x;
+        const int64_t v = i < ntiles ? tile_sums[i] : 0;
+        int64_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) sh[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            int64_t w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int64_t y = __shfl_up_sync(FULL, w, o);
+                if (lane >= o) w += y;
+            }
+            sh[lane] = w;
+        }
+        __syncthreads();
+        const int64_t warp_excl = wid ? sh[wid - 1] : 0;
+        if (i < ntiles) tile_sums[i] = carry + warp_excl + x - v;   // exclusive tile prefix
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += warp_excl + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int64_t R = carry;
+        if (R != p->nrefs) raise_status(p, w, ST_BAD_RANGE);
+        if (R > ref_cap) raise_status(p, w, ST_REF_CAP);
+        if (R >= INT32_MAX) raise_status(p, w, ST_TOO_BIG);
+        offsets[C] = (int32_t)R;
+    }
+}
+
+// In-place inclusive scan of each tile plus its prefix; queues cells that
+// hold two or more triangles for the segmented sort.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(int32_t* __restrict__ counts, GridParams* p,
+                                                                 const int64_t* __restrict__ tile_prefix,
+                                                                 BuildWork* w, int32_t* __restrict__ q_small,
+                                                                 int32_t* __restrict__ q_med,
+                                                                 int32_t* __restrict__ q_large, int64_t q_small_cap,
+                                                                 int64_t q_med_cap, int64_t q_large_cap) {
+    if (fatal(p->status)) return;
+    const int64_t C = p->ncells;
+    const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
+    __shared__ int64_t sh[9];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t b = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+        int32_t v[SCAN_ITEMS];
+        int64_t s = 0;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            v[i] = (b + i < C) ? counts[b + i] : 0;
+            s += v[i];
+        }
+        int64_t x = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) sh[wid] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int64_t run = 0;
+            for (int i = 0; i < SCAN_THREADS / 32; ++i) {
+                int64_t t = sh[i];
+                sh[i] = run;
+                run += t;
+            }
+        }
+        __syncthreads();
+        int64_t run = tile_prefix[tile] + sh[wid] + x - s;
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            if (b + i < C) {
+                run += v[i];
+                counts[b + i] = (int32_t)run;
+                const int32_t n = v[i];
+                if (n >= 2) {
+                    if (n <= 32) {
+                        const uint32_t slot = atomicAdd(&w->nsort[0], 1u);
+                        if (slot < q_small_cap) q_small[slot] = (int32_t)(b + i);
+                        else raise_status(p, w, ST_SORT_CAP);
+                    } else if (n <= 4096) {
+                        const uint32_t slot = atomicAdd(&w->nsort[1], 1u);
+                        if (slot < q_med_cap) q_med[slot] = (int32_t)(b + i);
+                        else raise_status(p, w, ST_SORT_CAP);
+                    } else {
+                        const uint32_t slot = atomicAdd(&w->nsort[2], 1u);
+                        if (slot < q_large_cap) q_large[slot] = (int32_t)(b + i);
+                        else raise_status(p, w, ST_SORT_CAP);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-cell sorts (after scatter, offsets[c] .. offsets[c+1] is cell c's list)
+// ---------------------------------------------------------------------------
+static __device__ __forceinline__ bool sort_skip(const GridParams* p) {
+    return (p->status & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP | ST_SORT_CAP)) != 0;
+}
+
+__global__ void __launch_bounds__(256) sort_small_kernel(const int32_t* __restrict__ offsets, int32_t* __restrict__ ids,
+                                                         const int32_t* __restrict__ q, const BuildWork* w,
+                                                         const GridParams* p) {
+    if (sort_skip(p)) return;
+    const uint32_t nq = w->nsort[0];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = warp; i < nq; i += nwarps) {
+        const int32_t c = q[i];
+        const int32_t s = offsets[c], n = offsets[c + 1] - s;
+        int32_t v = lane < n ? ids[s + lane] : INT_MAX;
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const int32_t o = __shfl_xor_sync(FULL, v, j);
+                const bool up = (lane & k) == 0;
+                const bool lower = (lane & j) == 0;
+                v = (lower == up) ? min(v, o) : max(v, o);
+            }
+        }
+        if (lane < n) ids[s + lane] = v;
+    }
+}
+
+static constexpr int MED_MAX = 4096;
+
+__global__ void __launch_bounds__(512) sort_medium_kernel(const int32_t* __restrict__ offsets,
+                                                          int32_t* __restrict__ ids, const int32_t* __restrict__ q,
+                                                          const BuildWork* w, const GridParams* p) {
+    if (sort_skip(p)) return;
+    __shared__ int32_t a[MED_MAX];
+    const uint32_t nq = w->nsort[1];
+    for (int64_t i = blockIdx.x; i < nq; i += gridDim.x) {
+        const int32_t c = q[i];
+        const int32_t s = offsets[c], n = offsets[c + 1] - s;
+        int m = 64;
+        while (m < n) m <<= 1;
+        for (int t = threadIdx.x; t < m; t += blockDim.x) a[t] = t < n ? ids[s + t] : INT_MAX;
+        __syncthreads();
+        for (int k = 2; k <= m; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int t = threadIdx.x; t < m; t += blockDim.x) {
+                    const int o = t ^ j;
+                    if (o > t) {
+                        const bool up = (t & k) == 0;
+                        const int32_t x = a[t], y = a[o];
+                        if ((x > y) == up) { a[t] = y; a[o] = x; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int t = threadIdx.x; t < n; t += blockDim.x) ids[s + t] = a[t];
+        __syncthreads();
+    }
+}
+
+// Cells above 4096 entries: copy the list to scratch, then per id chunk set
+// one shared-memory bit per id and write the set bits back in order.
+__global__ void __launch_bounds__(1024) sort_large_kernel(const int32_t* __restrict__ offsets,
+                                                          int32_t* __restrict__ ids, int32_t* __restrict__ scratch,
+                                                          const int32_t* __restrict__ q, const BuildWork* w,
+                                                          const GridParams* p, int32_t bitmap_words) {
+    if (sort_skip(p)) return;
+    extern __shared__ uint32_t bm[];
+    __shared__ int32_t sh_min[32], sh_max[32];
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t base_sh;
+    const uint32_t nq = w->nsort[2];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t qi = blockIdx.x; qi < nq; qi += gridDim.x) {
+        const int32_t c = q[qi];
+        const int32_t s = offsets[c], n = offsets[c + 1] - s;
+        int32_t mn = INT_MAX, mx = INT_MIN;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int32_t v = ids[s + t];
+            scratch[s + t] = v;
+            mn = min(mn, v);
+            mx = max(mx, v);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = min(mn, __shfl_xor_sync(FULL, mn, o));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, o));
+        }
+        if (lane == 0) { sh_min[wid] = mn; sh_max[wid] = mx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int i = 1; i < nw; ++i) { mn = min(mn, sh_min[i]); mx = max(mx, sh_max[i]); }
+            sh_min[0] = mn; sh_max[0] = mx;
+            base_sh = 0;
+        }
+        __syncthreads();
+        mn = sh_min[0];
+        mx = sh_max[0];
+        const int64_t span = (int64_t)bitmap_words * 32;
+        for (int64_t c0 = mn; c0 <= mx; c0 += span) {
+            for (int i = threadIdx.x; i < bitmap_words; i += blockDim.x) bm[i] = 0u;
+            __syncthreads();
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                const int64_t v = (int64_t)scratch[s + t] - c0;
+                if (v >= 0 && v < span) atomicOr(&bm[v >> 5], 1u << (v & 31));
+            }
+            __syncthreads();
+            // each thread owns a contiguous run of words
+            const int per = (bitmap_words + blockDim.x - 1) / blockDim.x;
+            const int w0 = threadIdx.x * per, w1 = min(w0 + per, bitmap_words);
+            int cnt = 0;
+            for (int i = w0; i < w1; ++i) cnt += __popc(bm[i]);
+            int x = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(FULL, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) warp_tot[wid] = x;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int run = 0;
+                for (int i = 0; i < nw; ++i) { const int t = warp_tot[i]; warp_tot[i] = run; run += t; }
+            }
+            __syncthreads();
+            int pos = s + base_sh + warp_tot[wid] + x - cnt;
+            for (int i = w0; i < w1; ++i) {
+                uint32_t bits = bm[i];
+                while (bits) {
+                    const int b = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    ids[pos++] = (int32_t)(c0 + (int64_t)i * 32 + b);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) base_sh += warp_tot[wid] + x;
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_build(const BuildArgs& a, cudaStream_t st) {
+    const int sms = a.num_sms;
+    count_launches(a.skip_bbox ? 9 : 10);
+    if (!a.skip_bbox) {
+        int64_t blocks = (a.nverts + 255) / 256;
+        blocks = blocks < 1 ? 1 : (blocks > 2 * sms ? 2 * sms : blocks);
+        bbox_params_kernel<<<(int)blocks, 256, 0, st>>>(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap);
+    }
+    {
+        int64_t blocks = (a.cell_cap / 4 + 255) / 256;
+        blocks = blocks < 1 ? 1 : (blocks > 8 * sms ? 8 * sms : blocks);
+        zero_offsets_kernel<<<(int)blocks, 256, 0, st>>>(a.offsets, a.params);
+    }
+    int64_t tri_blocks = (a.ntris + 255) / 256;   // one warp per 32 triangles
+    tri_blocks = tri_blocks < 1 ? 1 : (tri_blocks > 16 * sms ? 16 * sms : tri_blocks);
+    count_kernel<<<(int)tri_blocks, 256, 0, st>>>(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris);
+    int64_t tiles = (a.cell_cap + SCAN_TILE - 1) / SCAN_TILE;
+    tiles = tiles < 1 ? 1 : (tiles > 8 * sms ? 8 * sms : tiles);
+    scan_reduce_kernel<<<(int)tiles, SCAN_THREADS, 0, st>>>(a.offsets, a.params, a.tile_sums);
+    scan_tiles_kernel<<<1, 1024, 0, st>>>(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap);
+    scan_down_kernel<<<(int)tiles, SCAN_THREADS, 0, st>>>(a.offsets, a.params, a.tile_sums, a.work, a.q_small,
+                                                          a.q_med, a.q_large, a.q_small_cap, a.q_med_cap,
+                                                          a.q_large_cap);
+    scatter_kernel<<<(int)tri_blocks, 256, 0, st>>>(a.verts, a.idx, a.ntris, a.params, a.offsets, a.ids);
+    sort_small_kernel<<<8 * sms, 256, 0, st>>>(a.offsets, a.ids, a.q_small, a.work, a.params);
+    sort_medium_kernel<<<2 * sms, 512, 0, st>>>(a.offsets, a.ids, a.q_med, a.work, a.params);
+    sort_large_kernel<<<sms, 1024, (size_t)a.bitmap_words * 4, st>>>(a.offsets, a.ids, a.scratch, a.q_large, a.work,
+                                                                     a.params, a.bitmap_words);
+}
+
+cudaError_t build_setup_attributes(int bitmap_words) {
+    return cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bitmap_words * 4);
+}
+
+}  // namespace gridrt

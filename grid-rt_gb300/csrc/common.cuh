@@ -1,0 +1,96 @@
+// common.cuh -- shared device types and exact-rounding helpers.
+//
+// Parity-critical arithmetic (grid parameters, cell ranges, ray setup, box
+// clip, 3D-DDA) must round exactly like the reference's float code, which
+// evaluates every + - * / once in IEEE single precision
+// (src/rtplugins/UniformGridAccStruct.cpp:92-103,113-196,
+//  src/rtcore/AabbIntersection.cpp:37-63, include/rt/Ray.h:26-37).
+// The helpers below use the _rn intrinsics so nvcc can never contract them
+// into FMAs.  The Moller-Trumbore test is not bit-compared and may use FMA.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gridrt {
+
+// Grid parameters as UniformGridAccStruct holds them
+// (include/rtp/UniformGridAccStruct.h:49-56 + IAccStruct::_bbox).
+struct GridParams {
+    float bmin[3];
+    float bmax[3];
+    float cell[3];
+    float inv[3];
+    int32_t res[3];
+    int32_t k;
+    int64_t ncells;
+    int64_t nrefs;
+    int64_t ntris;
+    uint32_t status;
+    uint32_t pad;
+};
+
+// status bits written by the build kernels
+enum : uint32_t {
+    ST_CELL_CAP = 1u,     // ncells + 1 exceeds the offsets capacity
+    ST_REF_CAP = 2u,      // nrefs exceeds the ids capacity
+    ST_BAD_RANGE = 4u,    // a triangle's cell range fell outside the grid (non-finite input)
+    ST_AMBIGUOUS = 8u,    // resolution depends on the last ulp of powf: host recomputes
+    ST_TOO_BIG = 16u,     // ncells or nrefs beyond int32 (the reference's index type)
+    ST_SORT_CAP = 32u,    // segmented-sort work lists overflowed
+};
+
+// Work state shared by the build kernels of one scene (device memory).
+struct BuildWork {
+    uint32_t keys[6];        // ordered-int min xyz, max xyz
+    uint32_t ticket;         // last-block ticket of the bbox kernel
+    uint32_t nsort[3];       // cells queued for small / medium / large sorts
+    uint32_t sticky;         // OR of every build's status since the host last cleared it
+    uint32_t pad[5];
+};
+
+static constexpr float kHitEpsilon = 1e-4f;   // src/rtcore/RayTriIntersection.cpp:6
+static constexpr float kRayEpsilon = 2e-4f;   // src/rtcore/Context.cpp:505
+static constexpr float kFltMax = 3.402823466e+38f;
+
+// Sets status bits on the current build and on the sticky word.
+__device__ __forceinline__ void raise_status(GridParams* p, BuildWork* w, uint32_t bits) {
+    atomicOr(&p->status, bits);
+    if (w) atomicOr(&w->sticky, bits);
+}
+
+static __device__ __forceinline__ bool build_failed(uint32_t s) {
+    return (s & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP | ST_SORT_CAP | ST_BAD_RANGE)) != 0;
+}
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float frcp(float a) { return __frcp_rn(a); }
+// vr::min / vr::max / vr::abs semantics (a < b ? a : b etc.)
+__device__ __forceinline__ float vmin(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float vmax(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float vabs(float x) { return x < 0.0f ? -x : x; }
+__device__ __forceinline__ int32_t vclamp(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// UniformGridAccStruct::worldToVoxel (float -> int32 truncation toward zero)
+__device__ __forceinline__ int32_t world_to_voxel(float v, float bmin, float inv) {
+    return __float2int_rz(fmul(fsub(v, bmin), inv));
+}
+// UniformGridAccStruct::voxelToWorld
+__device__ __forceinline__ float voxel_to_world(int32_t vox, float cell, float bmin) {
+    return fadd(fmul(__int2float_rn(vox), cell), bmin);
+}
+
+// Monotone float <-> uint32 key for atomicMin / atomicMax.
+__device__ __forceinline__ uint32_t f2key(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(b);
+}
+
+}  // namespace gridrt

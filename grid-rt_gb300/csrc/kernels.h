@@ -1,0 +1,69 @@
+// kernels.h -- launchers shared by the host API (api.cu) and the kernel files.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace gridrt {
+
+struct BuildArgs {
+    const float* verts;
+    int64_t nverts;
+    const int32_t* idx;
+    int64_t ntris;
+    int32_t k;
+    bool skip_bbox;        // parameters already in `params` (host-resolved)
+    GridParams* params;
+    BuildWork* work;
+    float4* tris;          // 3 per triangle
+    int32_t* offsets;      // cell_cap entries
+    int64_t cell_cap;
+    int32_t* ids;          // ref_cap entries
+    int32_t* scratch;      // ref_cap entries
+    int64_t ref_cap;
+    int64_t* tile_sums;
+    int32_t* q_small;
+    int32_t* q_med;
+    int32_t* q_large;
+    int64_t q_small_cap, q_med_cap, q_large_cap;
+    int32_t bitmap_words;
+    int num_sms;
+};
+
+// Process-wide count of kernels launched by this library (diagnostics).
+void count_launches(int n);
+unsigned long long launches_so_far();
+
+void launch_build(const BuildArgs& a, cudaStream_t st);
+cudaError_t build_setup_attributes(int bitmap_words);
+
+// Read-only view of a built scene for the trace kernels.
+struct SceneView {
+    const GridParams* params;   // device
+    const int32_t* offsets;
+    const int32_t* ids;
+    const float4* tris;
+};
+
+struct CameraArgs {
+    float eye[3], base[3], nu[3], nv[3];
+    float inv_w, inv_h;
+    int32_t width, height, order;
+};
+
+struct TraceCounters {
+    unsigned long long rays, cells, tests;
+};
+
+void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
+                          int num_sms, cudaStream_t st);
+void launch_trace_any(const SceneView& s, const float4* rays, int64_t n, uint8_t* occ, TraceCounters* ctr,
+                      int num_sms, cudaStream_t st);
+void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
+                         float4* shadow_rays, TraceCounters* ctr, int num_sms, cudaStream_t st);
+void launch_deform(const float* base, const float* normals, float* out, int64_t nverts, float amp, float freq,
+                   float phase, cudaStream_t st);
+
+}  // namespace gridrt

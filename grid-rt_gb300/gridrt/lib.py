@@ -1,0 +1,280 @@
+"""ctypes binding of libgridrt.so (the C ABI in include/gridrt.h).
+
+This module is plumbing for Python callers (tests, bench): every compute call
+goes through the CUDA library.  Loading fails loudly when the library is
+missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+RTG_OK = 0
+RTG_NO_MEMORY = 1
+RTG_INVALID_PARAM = 3
+RTG_DEVICE_ERROR = 4
+RTG_TIMEOUT = 5
+RTG_NOT_BUILT = 6
+RTG_INVALID_GEOMETRY = 7
+
+RTG_TRACE_COUNTERS = 1
+ORDER = {"scanline": 0, "morton8": 1}
+
+
+class GridRTError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"gridrt status {status}: {msg}")
+        self.status = status
+
+
+class GridInfo(C.Structure):
+    _fields_ = [("res", C.c_int32 * 3), ("bmin", C.c_float * 3), ("bmax", C.c_float * 3), ("cell", C.c_float * 3),
+                ("inv_cell", C.c_float * 3), ("ncells", C.c_int64), ("nrefs", C.c_int64), ("k", C.c_int32),
+                ("built", C.c_int32)]
+
+    def as_dict(self):
+        return dict(res=tuple(self.res), bmin=np.array(self.bmin, np.float32), bmax=np.array(self.bmax, np.float32),
+                    cell=np.array(self.cell, np.float32), inv_cell=np.array(self.inv_cell, np.float32),
+                    ncells=int(self.ncells), nrefs=int(self.nrefs), k=int(self.k), built=bool(self.built))
+
+
+class CameraC(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("base_dir", C.c_float * 3), ("near_u", C.c_float * 3),
+                ("near_v", C.c_float * 3), ("width", C.c_int32), ("height", C.c_int32), ("order", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+def camera_struct(cam, order: str = "scanline") -> CameraC:
+    c = CameraC()
+    for a in range(3):
+        c.eye[a] = float(cam.eye[a])
+        c.base_dir[a] = float(cam.base_dir[a])
+        c.near_u[a] = float(cam.near_u[a])
+        c.near_v[a] = float(cam.near_v[a])
+    c.width, c.height, c.order = int(cam.width), int(cam.height), ORDER[order]
+    return c
+
+
+_lib = None
+EXPORTS = [
+    "rtg_version", "rtg_last_error", "rtg_scene_create", "rtg_scene_destroy", "rtg_scene_stream",
+    "rtg_scene_set_geometry", "rtg_scene_set_geometry_device", "rtg_scene_update_vertices",
+    "rtg_scene_deform_vertices", "rtg_scene_build", "rtg_scene_build_async", "rtg_scene_build_check",
+    "rtg_scene_reserve", "rtg_scene_grid_info", "rtg_scene_grid_download", "rtg_scene_download_vertices", "rtg_scene_grid_device",
+    "rtg_trace_nearest", "rtg_trace_nearest_device", "rtg_trace_any", "rtg_trace_any_device",
+    "rtg_trace_camera_device", "rtg_trace_frame_device", "rtg_trace_frame", "rtg_kernel_launch_count",
+    "rtg_scene_counters",
+]
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libgridrt.so (building it when absent and allowed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise FileNotFoundError(f"{path} missing: run __graft_entry__.build()")
+        _build.build()
+    L = C.CDLL(path)
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+    sig = {
+        "rtg_version": ([], C.c_char_p),
+        "rtg_last_error": ([], C.c_char_p),
+        "rtg_scene_create": ([C.c_int, vp, C.POINTER(vp)], C.c_int),
+        "rtg_scene_destroy": ([vp], C.c_int),
+        "rtg_scene_stream": ([vp, C.POINTER(vp)], C.c_int),
+        "rtg_scene_set_geometry": ([vp, vp, i64, vp, i64, vp], C.c_int),
+        "rtg_scene_set_geometry_device": ([vp, vp, i64, vp, i64, vp], C.c_int),
+        "rtg_scene_update_vertices": ([vp, vp, i64, C.c_int, vp], C.c_int),
+        "rtg_scene_deform_vertices": ([vp, vp, vp, C.c_float, C.c_float, C.c_float, vp], C.c_int),
+        "rtg_scene_build": ([vp, i32, vp], C.c_int),
+        "rtg_scene_build_async": ([vp, i32, vp], C.c_int),
+        "rtg_scene_build_check": ([vp, vp], C.c_int),
+        "rtg_scene_reserve": ([vp, i64, i64], C.c_int),
+        "rtg_scene_grid_info": ([vp, C.POINTER(GridInfo)], C.c_int),
+        "rtg_scene_grid_download": ([vp, vp, vp], C.c_int),
+        "rtg_scene_download_vertices": ([vp, vp], C.c_int),
+        "rtg_scene_grid_device": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)], C.c_int),
+        "rtg_trace_nearest": ([vp, vp, i64, vp, i32, vp], C.c_int),
+        "rtg_trace_nearest_device": ([vp, vp, i64, vp, i32, vp], C.c_int),
+        "rtg_trace_any": ([vp, vp, i64, vp, i32, vp], C.c_int),
+        "rtg_trace_any_device": ([vp, vp, i64, vp, i32, vp], C.c_int),
+        "rtg_trace_camera_device": ([vp, C.POINTER(CameraC), vp, vp, vp, i32, vp], C.c_int),
+        "rtg_trace_frame_device": ([vp, C.POINTER(CameraC), vp, vp, vp, vp, vp], C.c_int),
+        "rtg_trace_frame": ([vp, C.POINTER(CameraC), vp, vp, vp, vp], C.c_int),
+        "rtg_kernel_launch_count": ([], C.c_uint64),
+        "rtg_scene_counters": ([vp, C.POINTER(C.c_int64), C.c_int], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def check(rc: int):
+    if rc != RTG_OK:
+        raise GridRTError(rc, load().rtg_last_error().decode())
+
+
+def _ptr(a) -> int:
+    """Address of a numpy array or torch tensor."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class Scene:
+    """One geometry with its device-resident uniform grid."""
+
+    def __init__(self, device: int = 0, stream=None):
+        L = load()
+        h = C.c_void_p()
+        check(L.rtg_scene_create(int(device), stream, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().rtg_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(load().rtg_scene_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    # ---- geometry -----------------------------------------------------------
+    def set_geometry(self, verts: np.ndarray, idx: np.ndarray):
+        self._verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+        self._idx = np.ascontiguousarray(idx, np.int32).reshape(-1, 3)
+        self._nverts = self._verts.shape[0]
+        check(load().rtg_scene_set_geometry(self.h, _ptr(self._verts), self._verts.shape[0], _ptr(self._idx),
+                                            self._idx.shape[0], None))
+
+    def set_geometry_device(self, d_verts, nverts: int, d_idx, ntris: int, stream=None):
+        self._nverts = int(nverts)
+        check(load().rtg_scene_set_geometry_device(self.h, _ptr(d_verts), nverts, _ptr(d_idx), ntris, stream))
+
+    def update_vertices(self, verts, nverts: int, from_device: bool, stream=None):
+        check(load().rtg_scene_update_vertices(self.h, _ptr(verts), nverts, 1 if from_device else 0, stream))
+
+    def deform(self, d_base, d_normals, amp: float, freq: float, phase: float, stream=None):
+        check(load().rtg_scene_deform_vertices(self.h, _ptr(d_base), _ptr(d_normals), amp, freq, phase, stream))
+
+    # ---- grid ---------------------------------------------------------------
+    def build(self, k: int, stream=None):
+        check(load().rtg_scene_build(self.h, int(k), stream))
+
+    def build_async(self, k: int, stream=None):
+        check(load().rtg_scene_build_async(self.h, int(k), stream))
+
+    def build_check(self, stream=None) -> int:
+        return load().rtg_scene_build_check(self.h, stream)
+
+    def reserve(self, ncells: int, nrefs: int):
+        check(load().rtg_scene_reserve(self.h, int(ncells), int(nrefs)))
+
+    def info(self) -> dict:
+        gi = GridInfo()
+        check(load().rtg_scene_grid_info(self.h, C.byref(gi)))
+        return gi.as_dict()
+
+    def download(self):
+        inf = self.info()
+        off = np.empty(inf["ncells"] + 1, np.int32)
+        ids = np.empty(max(inf["nrefs"], 1), np.int32)
+        check(load().rtg_scene_grid_download(self.h, _ptr(off), _ptr(ids)))
+        return off, ids[:inf["nrefs"]]
+
+    def download_vertices(self) -> np.ndarray:
+        n = getattr(self, "_nverts", 0)
+        out = np.empty((n, 3), np.float32)
+        check(load().rtg_scene_download_vertices(self.h, _ptr(out)))
+        return out
+
+    def device_arrays(self):
+        o, i, t = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(load().rtg_scene_grid_device(self.h, C.byref(o), C.byref(i), C.byref(t)))
+        return o.value, i.value, t.value
+
+    # ---- tracing ------------------------------------------------------------
+    def trace_nearest(self, rays: np.ndarray, counters: bool = False) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hits = np.empty((rays.shape[0], 4), np.float32)
+        check(load().rtg_trace_nearest(self.h, _ptr(rays), rays.shape[0], _ptr(hits),
+                                       RTG_TRACE_COUNTERS if counters else 0, None))
+        return hits
+
+    def trace_any(self, rays: np.ndarray, counters: bool = False) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        occ = np.empty(rays.shape[0], np.uint8)
+        check(load().rtg_trace_any(self.h, _ptr(rays), rays.shape[0], _ptr(occ),
+                                   RTG_TRACE_COUNTERS if counters else 0, None))
+        return occ
+
+    def trace_nearest_device(self, d_rays, n: int, d_hits, counters: bool = False, stream=None):
+        check(load().rtg_trace_nearest_device(self.h, _ptr(d_rays), int(n), _ptr(d_hits),
+                                              RTG_TRACE_COUNTERS if counters else 0, stream))
+
+    def trace_any_device(self, d_rays, n: int, d_occ, counters: bool = False, stream=None):
+        check(load().rtg_trace_any_device(self.h, _ptr(d_rays), int(n), _ptr(d_occ),
+                                          RTG_TRACE_COUNTERS if counters else 0, stream))
+
+    def trace_camera_device(self, cam, d_hits, light=None, d_shadow_rays=None, order: str = "scanline",
+                            counters: bool = False, stream=None):
+        cs = camera_struct(cam, order)
+        lp = None
+        if light is not None:
+            self._light = np.ascontiguousarray(light, np.float32)
+            lp = _ptr(self._light)
+        check(load().rtg_trace_camera_device(self.h, C.byref(cs), _ptr(d_hits), lp, _ptr(d_shadow_rays),
+                                             RTG_TRACE_COUNTERS if counters else 0, stream))
+
+    def trace_frame_device(self, cam, light, d_hits, d_occ, d_shadow_rays, order: str = "scanline", stream=None):
+        cs = camera_struct(cam, order)
+        self._light = np.ascontiguousarray(light, np.float32)
+        check(load().rtg_trace_frame_device(self.h, C.byref(cs), _ptr(self._light), _ptr(d_hits), _ptr(d_occ),
+                                            _ptr(d_shadow_rays), stream))
+
+    def trace_frame(self, cam, light, hits_host, occ_host, order: str = "scanline", stream=None):
+        """Primary + shadow frame with host outputs (pinned buffers copy fastest)."""
+        cs = camera_struct(cam, order)
+        self._light = np.ascontiguousarray(light, np.float32)
+        check(load().rtg_trace_frame(self.h, C.byref(cs), _ptr(self._light), _ptr(hits_host), _ptr(occ_host),
+                                     stream))
+
+    def counters(self, reset: bool = True):
+        out = (C.c_int64 * 3)()
+        check(load().rtg_scene_counters(self.h, out, 1 if reset else 0))
+        return dict(rays=out[0], cells=out[1], tests=out[2])
+
+
+def kernel_launches() -> int:
+    return int(load().rtg_kernel_launch_count())
+
+
+def split_hits(hits: np.ndarray) -> dict:
+    hits = np.ascontiguousarray(hits).reshape(-1, 4)
+    h32 = hits.view(np.float32) if hits.dtype != np.float32 else hits
+    return dict(id=h32[:, 0].copy().view(np.int32), t=h32[:, 1].copy(), u=h32[:, 2].copy(), v=h32[:, 3].copy())

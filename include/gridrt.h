@@ -1,0 +1,202 @@
+/*
+ * gridrt.h -- C ABI of the GB300 uniform-grid ray tracer (libgridrt.so).
+ *
+ * Drop-in for the acceleration-structure path of potato3d/grid-rt:
+ *   rt::IAccStructBuilder::buildGeometry(Geometry*)          include/rt/IAccStructBuilder.h:16
+ *     implemented by rtp::UniformGridAccStructBuilder         src/rtplugins/UniformGridAccStructBuilder.cpp:58-149
+ *   rt::IAccStruct::traceNearestGeometry(Instance, Ray&, Hit&) include/rt/IAccStruct.h:22
+ *     implemented by rtp::UniformGridAccStruct               src/rtplugins/UniformGridAccStruct.cpp:30-42,113-196
+ *   rt::IAccStruct::traceAnyGeometry(...)                    include/rt/IAccStruct.h:28 (a stub in the reference)
+ * and of the CUDA tracer's host ABI (src/rtcuda/RayTracing.h:6-44), which this
+ * replaces with handles, status codes and caller-owned host arrays.
+ *
+ * Conventions
+ *  - Every call returns rtg_status.  Handles are opaque.  Host arrays stay
+ *    owned by the caller; device buffers are owned by the library.
+ *  - `stream` arguments are cudaStream_t passed as void*; NULL selects the
+ *    scene's own stream.  Calls on one scene are ordered on that stream;
+ *    trace calls on different streams may run concurrently once the scene is
+ *    built (the grid is read-only during tracing, as the reference requires
+ *    for its OpenMP renderers, src/rtplugins/MultiThreadRenderer.cpp:23-30).
+ *  - Rays: 8 x float32 per ray {ox, oy, oz, tnear, dx, dy, dz, tfar}
+ *    (rt::Ray orig/dir/tnear/tfar, include/rt/Ray.h:9-24).  The reference's
+ *    trace entry initialises tnear = 2e-4 and tfar = FLT_MAX
+ *    (src/rtcore/IAccStruct.cpp:33-36); callers that want that behaviour pass
+ *    those values.
+ *  - Hits: rtg_hit {id, t, u, v}; id = -1 for a miss.  u and v are the
+ *    barycentric weights of vertices 1 and 2 (Hit::v1Coord / v2Coord,
+ *    include/rt/Hit.h:9-17); the weight of vertex 0 is 1 - u - v.
+ *  - Geometry: vertices float32 x 3, triangle indices int32 x 3 (rt::Geometry
+ *    vertices + TriDesc::v, include/rt/Geometry.h:20-27).  Triangles must be
+ *    valid in the sense of TriAccel::valid (src/rtcore/Triangle.cpp:57-63), as
+ *    Context's PrimitiveBuilder guarantees before the builder runs.
+ */
+#ifndef GRIDRT_H
+#define GRIDRT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes; the first three keep the values of RT_OK / RT_NO_MEMORY /
+ * RT_INVALID_PARAM (include/rt/common.h:19-21). */
+typedef enum {
+    RTG_OK = 0,
+    RTG_NO_MEMORY = 1,
+    RTG_INVALID_PARAM = 3,
+    RTG_DEVICE_ERROR = 4,
+    RTG_TIMEOUT = 5,
+    RTG_NOT_BUILT = 6,
+    RTG_INVALID_GEOMETRY = 7
+} rtg_status;
+
+typedef struct rtg_scene_s* rtg_scene;
+
+typedef struct {
+    int32_t id;
+    float t;
+    float u;
+    float v;
+} rtg_hit;
+
+/* Grid description, as UniformGridAccStruct stores it
+ * (include/rtp/UniformGridAccStruct.h:49-56 plus IAccStruct::_bbox). */
+typedef struct {
+    int32_t res[3];
+    float bmin[3];
+    float bmax[3];
+    float cell[3];
+    float inv_cell[3];
+    int64_t ncells;
+    int64_t nrefs;
+    int32_t k;
+    int32_t built;
+} rtg_grid_info;
+
+/* Pinhole camera: the parameters of cudaSetCameraParameters
+ * (src/rtcuda/RayTracing.h:20-23) plus the viewport.  Ray for pixel (x, y),
+ * row 0 at the bottom: dir = base_dir + near_u*((x+0.5)/width) + near_v*((y+0.5)/height),
+ * unnormalised (src/rtplugins/PinholeCamera.cpp:131-137). */
+typedef struct {
+    float eye[3];
+    float base_dir[3];
+    float near_u[3];
+    float near_v[3];
+    int32_t width;
+    int32_t height;
+    int32_t order;   /* RTG_ORDER_* : mapping of ray index -> pixel */
+    int32_t pad;
+} rtg_camera;
+
+enum { RTG_ORDER_SCANLINE = 0, RTG_ORDER_MORTON8 = 1 };
+
+/* Flags for trace calls. */
+enum {
+    RTG_TRACE_DEFAULT = 0,
+    RTG_TRACE_COUNTERS = 1 /* accumulate cells visited / triangle tests (rtg_scene_counters) */
+};
+
+/* Library version and the device it runs on. */
+const char* rtg_version(void);
+/* Text of the last error on this thread. */
+const char* rtg_last_error(void);
+
+/* ---- scene lifetime ------------------------------------------------------
+ * rtg_scene_create: device ordinal, optional stream (NULL: the library
+ * creates a non-blocking stream for the scene).
+ * Replaces rtInitContext (src/rtcuda/RayTracing.h:8). */
+rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out);
+rtg_status rtg_scene_destroy(rtg_scene scene);
+/* The stream that NULL selects for this scene. */
+rtg_status rtg_scene_stream(rtg_scene scene, void** stream_out);
+
+/* ---- geometry ------------------------------------------------------------
+ * Copy vertices and triangles from HOST memory (cudaTransferTriangleVertices,
+ * src/rtcuda/RayTracing.h:27).  Sizes may change between calls. */
+rtg_status rtg_scene_set_geometry(rtg_scene scene, const float* verts, int64_t nverts, const int32_t* tris,
+                                  int64_t ntris, void* stream);
+/* Same, from DEVICE memory (no host round trip; the data is copied). */
+rtg_status rtg_scene_set_geometry_device(rtg_scene scene, const float* d_verts, int64_t nverts,
+                                         const int32_t* d_tris, int64_t ntris, void* stream);
+/* Replace vertex positions only (same vertex count), host or device source. */
+rtg_status rtg_scene_update_vertices(rtg_scene scene, const float* verts, int64_t nverts, int from_device,
+                                     void* stream);
+/* Displace every vertex along `normals` (float32 x 3 per vertex, device or
+ * host) by amp*sin(freq*p.x + phase) from the base positions `base`
+ * (device): the per-frame deformation of the deforming-mesh workload. */
+rtg_status rtg_scene_deform_vertices(rtg_scene scene, const float* d_base, const float* d_normals, float amp,
+                                     float freq, float phase, void* stream);
+
+/* ---- grid build (UniformGridAccStructBuilder::buildGeometry) -------------
+ * k = cells per triangle (the reference hard-codes 6,
+ * src/rtplugins/UniformGridAccStructBuilder.cpp:91).  Synchronous: returns
+ * after the grid is complete, growing device buffers as needed. */
+rtg_status rtg_scene_build(rtg_scene scene, int32_t k, void* stream);
+/* Asynchronous build for graph capture and pipelining: enqueues the build
+ * using the current buffer capacities.  rtg_scene_build_check synchronises the
+ * stream and returns RTG_OK, or RTG_NO_MEMORY when a capacity was exceeded
+ * (then call rtg_scene_build). */
+rtg_status rtg_scene_build_async(rtg_scene scene, int32_t k, void* stream);
+rtg_status rtg_scene_build_check(rtg_scene scene, void* stream);
+/* Reserve device capacity for grids of up to ncells cells and nrefs
+ * (cell, triangle) references (avoids regrowth inside captured graphs). */
+rtg_status rtg_scene_reserve(rtg_scene scene, int64_t ncells, int64_t nrefs);
+
+rtg_status rtg_scene_grid_info(rtg_scene scene, rtg_grid_info* out);
+/* Copy the CSR grid to host: offsets[ncells+1], ids[nrefs] (cell lists sorted
+ * by triangle id, linear cell index x + y*nx + z*nx*ny). */
+rtg_status rtg_scene_grid_download(rtg_scene scene, int32_t* offsets, int32_t* ids);
+/* Copy the scene's current vertex positions to host (nverts x 3 float32),
+ * e.g. after rtg_scene_deform_vertices. */
+rtg_status rtg_scene_download_vertices(rtg_scene scene, float* verts);
+/* Device pointers of the CSR grid and the triangle records (read-only use). */
+rtg_status rtg_scene_grid_device(rtg_scene scene, const int32_t** d_offsets, const int32_t** d_ids,
+                                 const float** d_tris);
+
+/* ---- tracing -------------------------------------------------------------
+ * Closest hit for n rays (UniformGridAccStruct::traceNearestGeometry).
+ * rays / hits in HOST memory: the call copies in and out and synchronises. */
+rtg_status rtg_trace_nearest(rtg_scene scene, const float* rays, int64_t n, rtg_hit* hits, int32_t flags,
+                             void* stream);
+/* rays / hits in DEVICE memory: asynchronous on `stream`. */
+rtg_status rtg_trace_nearest_device(rtg_scene scene, const float* d_rays, int64_t n, rtg_hit* d_hits,
+                                    int32_t flags, void* stream);
+/* Shadow any-hit: occluded[i] = 1 iff the ray hits a triangle before its
+ * tfar word (tmax).  HOST and DEVICE variants as above. */
+rtg_status rtg_trace_any(rtg_scene scene, const float* rays, int64_t n, uint8_t* occluded, int32_t flags,
+                         void* stream);
+rtg_status rtg_trace_any_device(rtg_scene scene, const float* d_rays, int64_t n, uint8_t* d_occluded,
+                                int32_t flags, void* stream);
+/* Camera rays generated on the device (cudaRayTrace, src/rtcuda/RayTracing.h:42),
+ * width*height closest hits into d_hits (ray i -> pixel per cam->order).
+ * With d_shadow_rays != NULL a shadow ray toward the point light is also
+ * written per pixel (SimplePointLight::illuminate, src/rtplugins/SimplePointLight.cpp:18-52;
+ * Sample::initLightRay/initShadowRay, src/rtcore/Sample.cpp:22-42): origin
+ * P + n*2e-4, direction light - origin (unnormalised), tnear 2e-4, tmax 1;
+ * pixels without a shadow ray (miss, or surface facing away from the light)
+ * get tmax = -1.  n is the flat normal turned to face the incoming ray. */
+rtg_status rtg_trace_camera_device(rtg_scene scene, const rtg_camera* cam, rtg_hit* d_hits,
+                                   const float* light_pos, float* d_shadow_rays, int32_t flags, void* stream);
+/* Primary + shadow frame: camera closest hits, shadow rays and any-hit in one
+ * call on the device.  occluded[i]: 0 lit, 1 shadowed, 2 no shadow ray. */
+rtg_status rtg_trace_frame_device(rtg_scene scene, const rtg_camera* cam, const float* light_pos,
+                                  rtg_hit* d_hits, uint8_t* d_occluded, float* d_shadow_rays, void* stream);
+
+/* The same frame with HOST outputs: copies hits (width*height rtg_hit) and
+ * occluded (width*height bytes) back and synchronises. */
+rtg_status rtg_trace_frame(rtg_scene scene, const rtg_camera* cam, const float* light_pos, rtg_hit* hits,
+                           uint8_t* occluded, void* stream);
+
+/* Number of CUDA kernels this library has launched in this process. */
+uint64_t rtg_kernel_launch_count(void);
+
+/* Counters accumulated by calls made with RTG_TRACE_COUNTERS since the last
+ * reset: out[0] = rays, out[1] = cells visited, out[2] = triangle tests. */
+rtg_status rtg_scene_counters(rtg_scene scene, int64_t out[3], int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

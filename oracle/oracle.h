@@ -1,0 +1,72 @@
+/*
+ * oracle.h -- CPU restatement of the reference's uniform-grid build and
+ * 3D-DDA trace (potato3d/grid-rt).  TEST INFRASTRUCTURE ONLY: tests, the
+ * smoke check and bench.py's CPU-baseline leg may load liboracle.so; the
+ * product (libgridrt.so) never links or calls it.
+ *
+ * Parity of this restatement is pinned against the reference's own sources
+ * compiled unmodified (oracle/_ref, built by `make ref` where the reference
+ * checkout exists) on seeded scenes, and against the committed golden
+ * fixtures in tests/golden/ that were produced by that compiled reference.
+ *
+ * Array conventions (all little-endian, row-major):
+ *   verts  : nverts x 3 float32
+ *   idx    : ntris  x 3 int32
+ *   rays   : n x 8 float32 {ox, oy, oz, tnear, dx, dy, dz, tfar}
+ *   hits   : n x 4 32-bit words {id (int32, -1 = miss), t, u, v}
+ *            u = Hit::v1Coord, v = Hit::v2Coord (src/rtcore/RayTriIntersection.cpp:43-47)
+ *   grid CSR: offsets[ncells + 1] int32, ids[nrefs] int32, linear cell index
+ *            x + y*nx + z*nx*ny (src/rtplugins/UniformGridAccStruct.cpp:82-90)
+ */
+#ifndef GRIDRT_ORACLE_H
+#define GRIDRT_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int32_t res[3];     /* nx, ny, nz */
+    float bmin[3];      /* grid box (scene box enlarged by 1%) */
+    float bmax[3];
+    float cell[3];      /* cell size */
+    float inv_cell[3];  /* 1 / cell size */
+    int64_t ncells;
+    int64_t nrefs;
+} orc_grid_info;
+
+/* Scene box, 1% enlargement and resolution rule with cells-per-triangle k.
+ * Returns 0 on success, nonzero for empty input. */
+int orc_grid_params(const float* verts, int64_t nverts, int64_t ntris, int32_t k, orc_grid_info* out);
+
+/* Full CSR build.  Call once with offsets == ids == NULL to obtain info
+ * (ncells, nrefs), then again with arrays of ncells+1 and nrefs entries. */
+int orc_grid_build(const float* verts, int64_t nverts, const int32_t* idx, int64_t ntris, int32_t k,
+                   orc_grid_info* info, int32_t* offsets, int32_t* ids);
+
+/* Wald projection records, 12 words per triangle (rt::TriAccel layout). */
+void orc_triaccel_build(const float* verts, const int32_t* idx, int64_t ntris, float* acc);
+
+/* Closest hit through the grid.  counters (optional) receives 2 int64 per
+ * ray: cells visited and triangle tests.  nthreads <= 0 uses all cores. */
+void orc_trace_closest(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc,
+                       const float* rays, int64_t n, float* hits, int64_t* counters, int nthreads);
+
+/* Shadow any-hit: occluded[i] = 1 iff the closest hit (tnear, tfar = tmax)
+ * exists with t < tmax, where tmax is the ray's tfar word. */
+void orc_trace_any(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc,
+                   const float* rays, int64_t n, uint8_t* occluded, int64_t* counters, int nthreads);
+
+/* Moller-Trumbore in double for (ray i, triangle tri[i]); out: n x 3 {t, u, v}
+ * (NaN where tri[i] < 0). */
+void orc_mt_f64(const float* verts, const int32_t* idx, const float* rays, const int32_t* tri, int64_t n,
+                double* out);
+
+/* Number of OpenMP threads the trace entry points use when nthreads <= 0. */
+int orc_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

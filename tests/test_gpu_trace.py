@@ -1,0 +1,136 @@
+"""GPU traversal vs the oracle: closest hit (id, t, u, v) under the near-tie
+rules of tests/parity.py, shadow any-hit, and bit-identical camera rays."""
+import numpy as np
+import pytest
+
+import parity
+from gridrt import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _scene(gridlib, sc, k):
+    s = gridlib.Scene(0)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(k)
+    return s
+
+
+def _report(name, st):
+    print(f"\n[{name}] " + ", ".join(f"{k}={v}" for k, v in st.items() if k != "unexplained_examples"))
+    if st["unexplained_examples"]:
+        print("  examples:", st["unexplained_examples"][:3])
+
+
+def test_plane_and_debris_primary(gridlib, oracle):
+    sc = scenes.plane_and_debris()
+    s = _scene(gridlib, sc, 4)
+    g = oracle.Grid(sc.verts, sc.idx, 4)
+    rays = scenes.camera_rays(scenes.plane_and_debris_camera())
+    gh = gridlib.split_hits(s.trace_nearest(rays))
+    oh = g.trace_closest(rays)
+    st = parity.compare_hits(gh, oh, sc.verts, sc.idx, rays, oracle)
+    _report("plane primary", st)
+    parity.assert_parity(st)
+
+
+def test_camera_kernel_matches_explicit_rays(gridlib, oracle):
+    import torch
+    sc = scenes.plane_and_debris()
+    s = _scene(gridlib, sc, 4)
+    for order in ("scanline", "morton8"):
+        cam = scenes.plane_and_debris_camera(256, 128)
+        rays = scenes.camera_rays(cam, order)
+        host = s.trace_nearest(rays).view(np.int32)
+        d_hits = torch.empty((rays.shape[0], 4), dtype=torch.int32, device="cuda")
+        s.trace_camera_device(cam, d_hits, order=order)
+        torch.cuda.synchronize()
+        dev = d_hits.cpu().numpy()
+        # identical rays give identical traversal, so every word matches
+        assert np.array_equal(host, dev), order
+
+
+def test_shadow_any_hit(gridlib, oracle):
+    import torch
+    sc = scenes.plane_and_debris()
+    s = _scene(gridlib, sc, 4)
+    g = oracle.Grid(sc.verts, sc.idx, 4)
+    cam = scenes.plane_and_debris_camera()
+    n = cam.width * cam.height
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    s.trace_frame_device(cam, scenes.PLANE_LIGHT, d_hits, d_occ, d_sr)
+    torch.cuda.synchronize()
+    occ = d_occ.cpu().numpy()
+    sr = d_sr.cpu().numpy()
+    hits = gridlib.split_hits(d_hits.cpu().numpy())
+    has = sr[:, 7] >= 0
+    assert (occ[~has] == 2).all()
+    assert (hits["id"][has] >= 0).all()
+    ref = g.trace_any(sr[has])
+    mism = int((occ[has] != ref).sum())
+    print(f"\n[shadow] rays={int(has.sum())} occluded={int(ref.sum())} mismatches={mism}")
+    assert mism <= max(1, int(1e-3 * has.sum()))
+    # the host any-hit entry point agrees with the fused frame call
+    occ2 = s.trace_any(sr[has])
+    assert np.array_equal(occ2, occ[has])
+
+
+@pytest.mark.parametrize("k", [2, 4, 8])
+def test_deforming_sphere_primary(gridlib, oracle, k):
+    sc = scenes.deforming_sphere(5)
+    s = _scene(gridlib, sc, k)
+    g = oracle.Grid(sc.verts, sc.idx, k)
+    rays = scenes.camera_rays(scenes.deforming_sphere_camera(512, 512))
+    gh = gridlib.split_hits(s.trace_nearest(rays))
+    oh = g.trace_closest(rays)
+    st = parity.compare_hits(gh, oh, sc.verts, sc.idx, rays, oracle)
+    _report(f"sphere k={k}", st)
+    parity.assert_parity(st)
+
+
+def test_random_rays_inside_box(gridlib, oracle):
+    sc = scenes.plane_and_debris()
+    s = _scene(gridlib, sc, 4)
+    g = oracle.Grid(sc.verts, sc.idx, 4)
+    rng = np.random.default_rng(7)
+    rays = scenes.random_rays(rng, 200_000, (-1.0, 0.0, -1.0), (1.0, 1.0, 1.0))
+    gh = gridlib.split_hits(s.trace_nearest(rays))
+    oh = g.trace_closest(rays)
+    st = parity.compare_hits(gh, oh, sc.verts, sc.idx, rays, oracle)
+    _report("random rays", st)
+    parity.assert_parity(st)
+    # any-hit with a finite tmax
+    rays[:, 7] = 0.3
+    occ = s.trace_any(rays)
+    ref = g.trace_any(rays)
+    assert (occ != ref).sum() <= max(1, int(1e-3 * rays.shape[0]))
+
+
+def test_skewed_density_subsample(gridlib, oracle):
+    sc = scenes.skewed_density()
+    s = _scene(gridlib, sc, 4)
+    g = oracle.Grid(sc.verts, sc.idx, 4)
+    rays = scenes.camera_rays(scenes.skewed_density_camera(256, 256))
+    gh = gridlib.split_hits(s.trace_nearest(rays))
+    oh = g.trace_closest(rays)
+    st = parity.compare_hits(gh, oh, sc.verts, sc.idx, rays, oracle)
+    _report("skewed", st)
+    parity.assert_parity(st)
+
+
+def test_counters_match_oracle(gridlib, oracle):
+    sc = scenes.plane_and_debris()
+    s = _scene(gridlib, sc, 4)
+    g = oracle.Grid(sc.verts, sc.idx, 4)
+    rays = scenes.camera_rays(scenes.plane_and_debris_camera())
+    s.counters(reset=True)
+    s.trace_nearest(rays, counters=True)
+    c = s.counters(reset=True)
+    _, oc = g.trace_closest(rays, counters=True)
+    # same DDA: cells visited equal exactly unless a near-tie ended a walk in
+    # a different cell
+    assert c["rays"] == rays.shape[0]
+    assert abs(c["cells"] - int(oc[:, 0].sum())) <= 1e-4 * oc[:, 0].sum()
+    assert abs(c["tests"] - int(oc[:, 1].sum())) <= 1e-3 * oc[:, 1].sum()
