@@ -53,9 +53,11 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while the
+    timed regions run; only samples whose timestamp falls inside a timed
+    window (mark()/unmark()) are summarised."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -63,24 +65,44 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.lines = []
+        self.windows = []
+        self._t0 = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t_end = time.time() + 5.0
+            while not self.lines and time.time() < t_end:   # wait for the first sample
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self
 
     def _read(self):
+        import datetime
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            parts = [p.strip() for p in line.split(",")]
+            try:
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except Exception:
+                ts = time.time()
+            self.lines.append((ts, parts))
 
-    def __exit__(self, *exc):
+    def mark(self):
+        self._t0 = time.time()
+
+    def unmark(self):
+        if self._t0 is not None:
+            self.windows.append((self._t0, time.time()))
+            self._t0 = None
+
+    def stop(self):
         if self.proc:
+            time.sleep(0.15)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -88,22 +110,22 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], 0.0, set()
+        sm, mx, reasons, n = [], 0.0, set(), 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+        for ts, parts in self.lines:
+            if len(parts) < 9 or not any(a - 0.05 <= ts <= b + 0.05 for a, b in self.windows):
                 continue
             try:
                 sm.append(float(parts[1]))
                 mx = max(mx, float(parts[2]))
             except ValueError:
                 continue
+            n += 1
             for nm, val in zip(names, parts[5:9]):
                 if val.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": n}
 
 
 def _dist():
@@ -209,7 +231,7 @@ def run_reference(args, rank, ws, dist):
     import pyoracle
     pyoracle.build()
     k = 4
-    stride = 16
+    stride = 4
     for w in range(args.warmup):
         cpu_frame_sample(k, w % FRAMES, stride)
     res = [cpu_frame_sample(k, s % FRAMES, stride) for s in range(args.steps)]
@@ -289,7 +311,7 @@ def run_gpu(args, rank, ws, local, dist):
     order = min(tune, key=tune.get)
 
     per_k = {}
-    launches0 = lib.kernel_launches()
+    sampler = ClockSampler(local).start() if rank == 0 else None
     for k in LAMBDAS:
         for w in range(args.warmup):
             frame(k, w % FRAMES, order)
@@ -300,9 +322,8 @@ def run_gpu(args, rank, ws, local, dist):
         shadow_count = torch.zeros((), dtype=torch.int64, device=dev)
         _barrier(dist)
         torch.cuda.synchronize()
-        sampler = ClockSampler(local) if (k == LAMBDAS[1] and rank == 0) else None
         if sampler:
-            sampler.__enter__()
+            sampler.mark()
         lc0 = lib.kernel_launches()
         for st in range(args.steps):
             with torch.cuda.stream(stream):
@@ -314,7 +335,7 @@ def run_gpu(args, rank, ws, local, dist):
         torch.cuda.synchronize()
         _barrier(dist)
         if sampler:
-            sampler.__exit__(None, None, None)
+            sampler.unmark()
         if s.build_check() != 0:
             raise RuntimeError("timed build failed: " + lib.load().rtg_last_error().decode())
         build_ms = [e[0].elapsed_time(e[1]) for e in evs]
@@ -328,7 +349,9 @@ def run_gpu(args, rank, ws, local, dist):
                         build_ms=statistics.median(build_ms), primary_ms=statistics.median(prim_ms),
                         shadow_ms=statistics.median(shad_ms), rays_per_step=rays / args.steps,
                         trace_mrays_s=rays / (sum(prim_ms) + sum(shad_ms)) / 1e3,
-                        launches=lc1 - lc0, clocks=sampler.summary() if sampler else None)
+                        launches=lc1 - lc0)
+    if sampler:
+        sampler.stop()
 
     best_k = max(per_k, key=lambda kk: per_k[kk]["value"])
     head = per_k[best_k]
@@ -361,8 +384,11 @@ def run_gpu(args, rank, ws, local, dist):
 
     if rank != 0:
         return
-    cpu = cpu_frame_sample(best_k, 0, 16)
-    clocks = per_k[LAMBDAS[1]]["clocks"] or {}
+    cpu_frames = [cpu_frame_sample(best_k, f, 1) for f in range(0, FRAMES, 2)]   # 10 frames, every ray
+    cpu = dict(t_build=statistics.median(c["t_build"] for c in cpu_frames),
+               t_frame=sum(c["t_frame"] for c in cpu_frames), rays=sum(c["rays"] for c in cpu_frames),
+               threads=cpu_frames[0]["threads"])
+    clocks = sampler.summary() if sampler else {}
     out = {
         "metric": METRIC, "value": round(head["value"], 3), "unit": "Mrays/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4),
@@ -371,7 +397,7 @@ def run_gpu(args, rank, ws, local, dist):
                    "rays_primary": npix, "l2": "flushed between frames (256 MiB write, outside the timed events)",
                    "parallelism": f"replicas x{ws}"},
         "build_ms": round(head["build_ms"], 4), "trace_mrays_s": round(head["trace_mrays_s"], 2),
-        "per_k": {str(kk): {x: (round(y, 4) if isinstance(y, float) else y) for x, y in d.items() if x != "clocks"}
+        "per_k": {str(kk): {x: (round(y, 4) if isinstance(y, float) else y) for x, y in d.items()}
                   for kk, d in per_k.items()},
         "order_tune_ms": {o: round(t, 4) for o, t in tune.items()},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -380,8 +406,9 @@ def run_gpu(args, rank, ws, local, dist):
                      "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"])},
         "cpu_baseline": {"value": round(cpu["rays"] / cpu["t_frame"] / 1e6, 4), "unit": "Mrays/s",
                          "cores": cpu["threads"], "kind": "port",
-                         "sample": f"frame 0, k={best_k}: single-thread grid build + every 16th primary ray and its "
-                                   f"shadow ray on {cpu['threads']} threads, trace time x16",
+                         "sample": f"10 of the 20 frames, k={best_k}: single-thread grid build (as the reference "
+                                   f"builds) + all 1024^2 primary rays and their shadow rays on {cpu['threads']} "
+                                   f"threads; value = rays / (build + trace) time",
                          "build_ms": round(cpu["t_build"] * 1e3, 3)},
         "e2e": e2e,
         "gpu_launches": int(head["launches"]),
@@ -434,7 +461,7 @@ def run_e2e(args, s, v, idx, nrm, cam, light, k, order, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
     args = ap.parse_args()

@@ -144,6 +144,11 @@ BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
 // float operation order as src/rtplugins/UniformGridAccStructBuilder.cpp:86-98
 // and src/rtplugins/UniformGridAccStruct.cpp:56-62 (compiled without FMA
 // contraction).
+}  // namespace
+
+namespace gridrt {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap) {
     volatile float diag[3];
     for (int d = 0; d < 3; ++d) diag[d] = p.bmax[d] - p.bmin[d];
@@ -176,6 +181,9 @@ void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap) {
     p.ntris = ntris;
     p.status = st;
 }
+}  // namespace gridrt
+
+namespace {
 
 rtg_status read_params(rtg_scene s) {
     CUDA_TRY(cudaMemcpyAsync(s->h_params, s->d_params, sizeof(GridParams), cudaMemcpyDeviceToHost, s->stream));
@@ -385,12 +393,15 @@ rtg_status rtg_scene_build_async(rtg_scene s, int32_t k, void* stream) {
     if (rc) return rc;
     s->k = k;
     if (s->ntris == 0 || s->nverts == 0) return empty_grid(s, k);
-    if (!s->d_offsets) {
-        rc = ensure_grid_buffers(s, 1, 1);
-        if (rc) return rc;
-    }
-    s->built = false;
-    return enqueue_build(s, k, false, pick(s, stream));
+    // The first build of a scene runs synchronously: it sizes the buffers.
+    if (!s->d_offsets || s->hp.ncells == 0) return rtg_scene_build(s, k, stream);
+    rc = enqueue_build(s, k, false, pick(s, stream));
+    if (rc) return rc;
+    // Trace calls may follow on the same stream: the trace kernels read the
+    // device-side status and return misses if this build failed, and
+    // rtg_scene_build_check reports the failure.
+    s->built = true;
+    return RTG_OK;
 }
 
 rtg_status rtg_scene_build_check(rtg_scene s, void* stream) {

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -37,6 +38,11 @@ void count_launches(int n);
 unsigned long long launches_so_far();
 
 void launch_build(const BuildArgs& a, cudaStream_t st);
+// Host resolution of the grid parameters with the C library's powf (used when
+// the device flags ST_AMBIGUOUS); defined in api.cu.
+void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap);
+// Sets the text rtg_last_error() returns on this thread; defined in api.cu.
+void set_last_error(const std::string& msg);
 cudaError_t build_setup_attributes(int bitmap_words);
 
 // Read-only view of a built scene for the trace kernels.

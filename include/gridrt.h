@@ -135,9 +135,11 @@ rtg_status rtg_scene_deform_vertices(rtg_scene scene, const float* d_base, const
  * after the grid is complete, growing device buffers as needed. */
 rtg_status rtg_scene_build(rtg_scene scene, int32_t k, void* stream);
 /* Asynchronous build for graph capture and pipelining: enqueues the build
- * using the current buffer capacities.  rtg_scene_build_check synchronises the
- * stream and returns RTG_OK, or RTG_NO_MEMORY when a capacity was exceeded
- * (then call rtg_scene_build). */
+ * using the current buffer capacities (the first build of a scene runs
+ * synchronously to size them).  Trace calls may be enqueued right after it on
+ * the same stream.  rtg_scene_build_check synchronises the stream and returns
+ * RTG_OK, or RTG_NO_MEMORY when any build since the last check exceeded a
+ * capacity (its traces returned misses; call rtg_scene_build). */
 rtg_status rtg_scene_build_async(rtg_scene scene, int32_t k, void* stream);
 rtg_status rtg_scene_build_check(rtg_scene scene, void* stream);
 /* Reserve device capacity for grids of up to ncells cells and nrefs

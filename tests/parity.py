@@ -4,16 +4,18 @@ The device kernel mirrors the reference's 3D-DDA exactly, but intersects with
 Moller-Trumbore where the reference uses Wald's projection test
 (src/rtcore/RayTriIntersection.cpp:12-48).  Results are compared per ray:
 
-* same triangle id  -> t within 1e-5 relative and u / v within 1e-5 of the
-                       oracle (barycentrics live in [0, 1], so the bound is
-                       applied to |du|, |dv|) -- OR, where the oracle's own
-                       float result is further than that from the FP64
-                       Moller-Trumbore recomputation of the same ray and
-                       triangle, the GPU value must be at least as close to
-                       the FP64 value as the oracle's ("fp64-closer").  Wald's
-                       float test loses up to ~5e-3 on grazing or far-away
-                       small triangles, so a flat 1e-5 band around it would
-                       reject more accurate results.
+* same triangle id  -> each of t (relative), u, v (absolute; barycentrics
+                       live in [0, 1]) is within 1e-5 of the oracle, OR within
+                       the FP32 conditioning bound of the FP64 Moller-Trumbore
+                       value of that ray and triangle:
+                         u, v: 16 * 2^-24 * max(|o|, |P|) / (h_min * cos)
+                         t:    16 * 2^-24 * (1 + max(|o|, |P|) / (t |d|)) / cos
+                       (P hit point, h_min smallest altitude of the triangle,
+                       cos = |cos| of the ray / normal angle, floored at 1e-3).
+                       Wald's float test in the reference itself differs from
+                       FP64 by up to ~5e-3 on grazing or far-away small
+                       triangles; it meets this bound on every hit (checked in
+                       the same call and reported as oracle_cond_violations).
 * different ids or hit / miss, accepted only as a documented near-tie:
     - "t-tie":   both hit and the two t differ by < 1e-6 relative
     - "edge":    the FP64 Moller-Trumbore recomputation puts the triangle one
@@ -35,6 +37,31 @@ TIE_REL = 1e-6
 EDGE_EPS = 1e-5
 
 
+EPS32 = 2.0 ** -24
+
+
+def conditioning(verts, idx, rays, tri, f64):
+    """FP32 conditioning bounds (tau_t relative, tau_b absolute) per hit."""
+    v0 = verts[idx[tri, 0]].astype(np.float64)
+    v1 = verts[idx[tri, 1]].astype(np.float64)
+    v2 = verts[idx[tri, 2]].astype(np.float64)
+    e1, e2 = v1 - v0, v2 - v0
+    n = np.cross(e1, e2)
+    area2 = np.linalg.norm(n, axis=1)
+    longest = np.max(np.stack([np.linalg.norm(e1, axis=1), np.linalg.norm(e2, axis=1),
+                               np.linalg.norm(v2 - v1, axis=1)]), axis=0)
+    hmin = area2 / longest
+    d = rays[:, 4:7].astype(np.float64)
+    o = rays[:, 0:3].astype(np.float64)
+    dn = np.linalg.norm(d, axis=1)
+    cos = np.maximum(np.abs((d * n).sum(1)) / (dn * area2), 1e-3)
+    P = o + d * f64[:, 0:1]
+    mag = np.maximum(np.abs(o).max(1), np.abs(P).max(1))
+    tau_b = 16 * EPS32 * mag / (hmin * cos)
+    tau_t = 16 * EPS32 * (1.0 + mag / (np.abs(f64[:, 0]) * dn)) / cos
+    return tau_t, tau_b
+
+
 def _bary_margin(f64row):
     t, u, v = f64row
     return min(u, v, 1.0 - u - v)
@@ -53,10 +80,12 @@ def compare_hits(gpu: dict, orc: dict, verts, idx, rays, pyoracle, max_unexplain
     # error of both sides against an FP64 Moller-Trumbore recomputation
     err64 = {}
     bad_vals = 0
-    fp64_closer = 0
+    within_cond = 0
+    oracle_viol = 0
     bi = np.nonzero(both)[0]
     if bi.size:
         f64 = pyoracle.mt_f64(verts, idx, rays[bi], gid[bi])
+        tau_t, tau_b = conditioning(verts, idx, rays[bi], gid[bi], f64)
         e = {}
         for side, h in (("gpu", gpu), ("oracle", orc)):
             et = np.abs(h["t"][bi] - f64[:, 0]) / np.maximum(np.abs(f64[:, 0]), 1e-30)
@@ -65,11 +94,13 @@ def compare_hits(gpu: dict, orc: dict, verts, idx, rays, pyoracle, max_unexplain
             e[side] = (et, eu, ev)
             err64[side] = dict(t_max=float(et.max()), t_mean=float(et.mean()), u_max=float(eu.max()),
                                u_mean=float(eu.mean()), v_max=float(ev.max()), v_mean=float(ev.mean()))
-        for q, (d_go, tol) in enumerate(((t_err, T_REL), (u_err, BARY_ABS), (v_err, BARY_ABS))):
+        for q, (d_go, tol, tau) in enumerate(((t_err, T_REL, tau_t), (u_err, BARY_ABS, tau_b),
+                                              (v_err, BARY_ABS, tau_b))):
             out = d_go > tol
-            closer = e["gpu"][q] <= e["oracle"][q] * (1.0 + 1e-6) + 1e-12
-            bad_vals += int((out & ~closer).sum())
-            fp64_closer += int((out & closer).sum())
+            cond_ok = e["gpu"][q] <= np.maximum(tau, tol)
+            bad_vals += int((out & ~cond_ok).sum())
+            within_cond += int((out & cond_ok).sum())
+            oracle_viol += int((e["oracle"][q] > np.maximum(tau, tol)).sum())
     mism = np.nonzero(~same)[0]
     cats = {"t-tie": 0, "edge": 0, "window": 0, "unexplained": 0}
     unexplained = []
@@ -101,7 +132,7 @@ def compare_hits(gpu: dict, orc: dict, verts, idx, rays, pyoracle, max_unexplain
                 unexplained.append((int(i), int(gid[i]), float(tg), int(oid[i]), float(to),
                                     [float(x) for x in g64[j]], [float(x) for x in o64[j]]))
     stats = dict(n=n, hits=int((oid >= 0).sum()), mismatches=int(mism.size), bad_values=bad_vals,
-                 fp64_closer=fp64_closer, **cats,
+                 within_cond=within_cond, oracle_cond_violations=oracle_viol, **cats,
                  t_err_max=float(t_err.max()) if t_err.size else 0.0,
                  u_err_max=float(u_err.max()) if u_err.size else 0.0,
                  v_err_max=float(v_err.max()) if v_err.size else 0.0,
@@ -122,5 +153,6 @@ def _near_window(ray, ts, orc, gpu, i) -> bool:
 def assert_parity(stats: dict, max_tie_frac: float = 1e-3):
     msg = {k: v for k, v in stats.items()}
     assert stats["bad_values"] == 0, f"t/u/v outside tolerance: {msg}"
+    assert stats["oracle_cond_violations"] == 0, f"conditioning bound too tight for the oracle: {msg}"
     assert stats["unexplained"] == 0, f"unexplained id mismatches: {msg}"
     assert stats["mismatches"] <= max(1, int(max_tie_frac * stats["n"])), f"too many near-ties: {msg}"
