@@ -66,7 +66,8 @@ EXPORTS = [
     "rtg_scene_deform_vertices", "rtg_scene_build", "rtg_scene_build_async", "rtg_scene_build_check",
     "rtg_scene_reserve", "rtg_scene_grid_info", "rtg_scene_grid_download", "rtg_scene_download_vertices", "rtg_scene_grid_device",
     "rtg_trace_nearest", "rtg_trace_nearest_device", "rtg_trace_any", "rtg_trace_any_device",
-    "rtg_trace_camera_device", "rtg_trace_frame_device", "rtg_trace_frame", "rtg_kernel_launch_count",
+    "rtg_trace_camera_device", "rtg_trace_frame_device", "rtg_trace_frame", "rtg_grid_build_noalloc",
+    "rtg_kernel_launch_count",
     "rtg_scene_counters",
 ]
 
@@ -112,6 +113,8 @@ def load(build_if_missing: bool = True):
         "rtg_trace_camera_device": ([vp, C.POINTER(CameraC), vp, vp, vp, i32, vp], C.c_int),
         "rtg_trace_frame_device": ([vp, C.POINTER(CameraC), vp, vp, vp, vp, vp], C.c_int),
         "rtg_trace_frame": ([vp, C.POINTER(CameraC), vp, vp, vp, vp], C.c_int),
+        "rtg_grid_build_noalloc": ([vp, i64, vp, i64, i32, vp, i64, vp, i64, vp, C.POINTER(GridInfo), vp],
+                                   C.c_int),
         "rtg_kernel_launch_count": ([], C.c_uint64),
         "rtg_scene_counters": ([vp, C.POINTER(C.c_int64), C.c_int], C.c_int),
     }

@@ -191,6 +191,30 @@ rtg_status rtg_trace_frame_device(rtg_scene scene, const rtg_camera* cam, const 
 rtg_status rtg_trace_frame(rtg_scene scene, const rtg_camera* cam, const float* light_pos, rtg_hit* hits,
                            uint8_t* occluded, void* stream);
 
+/* Grid build that allocates no device memory.  It has no counterpart in the
+ * reference; it exists for callers that must not let a library allocate GPU
+ * memory: real-time frame loops, where an allocation and the synchronisation
+ * it can bring would stall the frame, and applications that hand out every
+ * byte of device memory from their own pool or allocator.
+ * The caller passes device arrays: d_verts (nverts x 3 float32), d_tris
+ * (ntris x 3 int32) and the outputs d_offsets (offsets_cap int32, 16-byte
+ * aligned; the grid needs ncells + 1), d_ids (ids_cap int32; nrefs needed) and
+ * d_tri_records (ntris x 12 float32, 16-byte aligned: v0|id, e1, e2).  The
+ * result equals rtg_scene_build's grid bit for bit; *info receives the grid
+ * description (also on RTG_NO_MEMORY, so the caller can size its buffers and
+ * call again).  The build's working memory is one fixed device array inside
+ * the library (about 3.2 MB on every GPU that loads the library, kept until
+ * the process exits): at most 524,288 (cell, triangle) references and
+ * 16,777,216 cells per call; larger grids return RTG_INVALID_PARAM.  The call
+ * synchronises `stream` before returning.  All calls share that array: each
+ * call clears what must start from zero, and calls that overlap on the GPU
+ * (different streams or threads at once) race -- serialise them.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress) with
+ * that device current; make it before any stream capture on that device. */
+rtg_status rtg_grid_build_noalloc(const float* d_verts, int64_t nverts, const int32_t* d_tris, int64_t ntris,
+                                  int32_t k, int32_t* d_offsets, int64_t offsets_cap, int32_t* d_ids,
+                                  int64_t ids_cap, float* d_tri_records, rtg_grid_info* info, void* stream);
+
 /* Number of CUDA kernels this library has launched in this process. */
 uint64_t rtg_kernel_launch_count(void);
 
