@@ -10,6 +10,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/gridrt.h"
 #include "common.cuh"
@@ -49,46 +50,7 @@ cudaError_t grow(T*& p, int64_t& cap, int64_t need) {
 
 }  // namespace
 
-struct rtg_scene_s {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int num_sms = 0;
-
-    float* d_verts = nullptr;
-    int64_t verts_cap = 0, nverts = 0;   // capacity in floats
-    int32_t* d_idx = nullptr;
-    int64_t idx_cap = 0, ntris = 0;      // capacity in ints
-    float4* d_tris = nullptr;
-    int64_t tris_cap = 0;                // float4 records
-
-    GridParams* d_params = nullptr;
-    GridParams* h_params = nullptr;      // pinned mirror
-    BuildWork* d_work = nullptr;
-    int32_t* d_offsets = nullptr;
-    int64_t cell_cap = 0;
-    int32_t* d_ids = nullptr;
-    int64_t ids_cap = 0;
-    int32_t* d_scratch = nullptr;
-    int64_t scratch_cap = 0;
-    int64_t* d_tiles = nullptr;
-    int64_t tiles_cap = 0;
-    int32_t* d_qs = nullptr;
-    int64_t qs_cap = 0;
-    int32_t* d_qm = nullptr;
-    int64_t qm_cap = 0;
-    int32_t* d_ql = nullptr;
-    int64_t ql_cap = 0;
-    int32_t bitmap_words = 32768;
-
-    bool built = false;
-    int32_t k = 0;
-    GridParams hp{};   // host copy of the last successful build
-
-    unsigned char* d_io = nullptr;
-    int64_t io_cap = 0;
-    TraceCounters* d_ctr = nullptr;
-};
+#include "scene.h"
 
 namespace {
 
@@ -101,6 +63,7 @@ int64_t ref_capacity(const rtg_scene s) { return s->ids_cap < s->scratch_cap ? s
 
 rtg_status ensure_grid_buffers(rtg_scene s, int64_t cells_plus_one, int64_t refs) {
     CUDA_TRY(grow(s->d_offsets, s->cell_cap, cells_plus_one));
+    CUDA_TRY(grow(s->d_occ, s->occ_cap, s->cell_cap));
     CUDA_TRY(grow(s->d_tiles, s->tiles_cap, s->cell_cap / 4096 + 2));
     CUDA_TRY(grow(s->d_ids, s->ids_cap, refs));
     CUDA_TRY(grow(s->d_scratch, s->scratch_cap, refs));
@@ -123,7 +86,8 @@ BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
     a.work = s->d_work;
     a.tris = s->d_tris;
     a.offsets = s->d_offsets;
-    a.cell_cap = s->cell_cap;
+    a.occ = s->d_occ;
+    a.cell_cap = s->cell_cap < s->occ_cap ? s->cell_cap : s->occ_cap;
     a.ids = s->d_ids;
     a.scratch = s->d_scratch;
     a.ref_cap = ref_capacity(s);
@@ -218,14 +182,36 @@ rtg_status empty_grid(rtg_scene s, int32_t k) {
 
 cudaStream_t pick(rtg_scene s, void* stream) { return stream ? (cudaStream_t)stream : s->stream; }
 
-SceneView view(rtg_scene s) {
+}  // namespace
+
+namespace gridrt {
+// Each trace launch takes the next of kRayCounters device words for its ray
+// hand-out, so up to that many launches may be in flight at once.
+unsigned long long* scene_counter(rtg_scene s) {
+    const unsigned slot = __atomic_fetch_add(&s->ctr_seq, 1u, __ATOMIC_RELAXED) % kRayCounters;
+    return s->d_ray_ctr + slot;
+}
+}  // namespace gridrt
+
+namespace {
+unsigned long long* next_counter(rtg_scene s) { return scene_counter(s); }
+
+}  // namespace
+
+namespace gridrt {
+SceneView scene_view(rtg_scene s) {
     SceneView v;
     v.params = s->d_params;
     v.offsets = s->d_offsets;
     v.ids = s->d_ids;
+    v.occ = s->d_occ;
     v.tris = s->d_tris;
     return v;
 }
+}  // namespace gridrt
+
+namespace {
+SceneView view(rtg_scene s) { return scene_view(s); }
 
 rtg_status ensure_io(rtg_scene s, int64_t bytes) {
     if (bytes <= s->io_cap && s->d_io) return RTG_OK;
@@ -271,6 +257,8 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
     if (rc == RTG_OK && cudaMallocHost(&s->h_params, sizeof(GridParams)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "pinned");
     if (rc == RTG_OK && cudaMalloc(&s->d_work, sizeof(BuildWork)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "work");
     if (rc == RTG_OK && cudaMalloc(&s->d_ctr, sizeof(TraceCounters)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "ctr");
+    if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
+        rc = fail(RTG_NO_MEMORY, "ray counters");
     if (rc == RTG_OK) {
         BuildWork w;
         std::memset(&w, 0, sizeof(w));
@@ -299,6 +287,8 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
     if (s->h_params) cudaFreeHost(s->h_params);
     cudaFree(s->d_work);
     cudaFree(s->d_offsets);
+    cudaFree(s->d_occ);
+    cudaFree(s->d_ray_ctr);
     cudaFree(s->d_ids);
     cudaFree(s->d_scratch);
     cudaFree(s->d_tiles);
@@ -557,7 +547,7 @@ rtg_status rtg_trace_nearest_device(rtg_scene s, const float* d_rays, int64_t n,
         return RTG_OK;
     }
     launch_trace_nearest(view(s), reinterpret_cast<const float4*>(d_rays), n, reinterpret_cast<int4*>(d_hits),
-                         (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, s->num_sms, st);
+                         (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, next_counter(s), s->tune, s->num_sms, st);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;
 }
@@ -574,7 +564,7 @@ rtg_status rtg_trace_any_device(rtg_scene s, const float* d_rays, int64_t n, uin
         return RTG_OK;
     }
     launch_trace_any(view(s), reinterpret_cast<const float4*>(d_rays), n, d_occ,
-                     (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, s->num_sms, st);
+                     (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, next_counter(s), s->tune, s->num_sms, st);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;
 }
@@ -655,7 +645,28 @@ rtg_status rtg_trace_camera_device(rtg_scene s, const rtg_camera* cam, rtg_hit* 
     }
     launch_trace_camera(view(s), camera_args(cam), reinterpret_cast<int4*>(d_hits), light_pos,
                         reinterpret_cast<float4*>(d_shadow_rays), (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr,
-                        s->num_sms, st);
+                        next_counter(s), s->tune, s->num_sms, st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_camera_diffuse_device(rtg_scene s, const rtg_camera* cam, uint64_t seed, rtg_hit* d_hits,
+                                           float* d_secondary_rays, int32_t flags, void* stream) {
+    rtg_status rc = check_traceable(s, 0);
+    if (rc) return rc;
+    if (!camera_ok(cam)) return fail(RTG_INVALID_PARAM, "bad camera (size, or Morton order needs multiples of 8)");
+    if (!d_hits || !d_secondary_rays) return fail(RTG_INVALID_PARAM, "NULL arrays");
+    cudaStream_t st = pick(s, stream);
+    const int64_t n = (int64_t)cam->width * cam->height;
+    if (s->hp.ncells == 0) {
+        CUDA_TRY(cudaMemsetAsync(d_hits, 0xff, sizeof(rtg_hit) * n, st));
+        CUDA_TRY(cudaMemsetAsync(d_secondary_rays, 0xff, 32 * n, st));
+        return RTG_OK;
+    }
+    launch_trace_camera(view(s), camera_args(cam), reinterpret_cast<int4*>(d_hits), nullptr,
+                        reinterpret_cast<float4*>(d_secondary_rays),
+                        (flags & RTG_TRACE_COUNTERS) ? s->d_ctr : nullptr, next_counter(s), s->tune, s->num_sms,
+                        st, 1, (unsigned long long)seed);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;
 }
@@ -671,7 +682,8 @@ rtg_status rtg_trace_frame_device(rtg_scene s, const rtg_camera* cam, const floa
         CUDA_TRY(cudaMemsetAsync(d_occ, 2, n, st));
         return RTG_OK;
     }
-    launch_trace_any(view(s), reinterpret_cast<const float4*>(d_shadow_rays), n, d_occ, nullptr, s->num_sms, st);
+    launch_trace_any(view(s), reinterpret_cast<const float4*>(d_shadow_rays), n, d_occ, nullptr, next_counter(s),
+                     s->tune, s->num_sms, st);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;
 }
@@ -698,6 +710,225 @@ rtg_status rtg_trace_frame(rtg_scene s, const rtg_camera* cam, const float* ligh
 }
 
 uint64_t rtg_kernel_launch_count(void) { return (uint64_t)launches_so_far(); }
+
+}  // extern "C"
+
+struct rtg_batch_s {
+    int device = 0;
+    int num_sms = 0;
+    std::vector<rtg_scene> scenes;
+    std::vector<int32_t> k;
+    std::vector<BuildArgs> h_build;       // host copies, to detect changed buffers
+    std::vector<BatchScene> h_scenes;
+    BuildArgs* d_build = nullptr;
+    BatchScene* d_scenes = nullptr;
+    BatchTask* d_tasks = nullptr;
+    int ntasks = 0;
+    long long total = 0;                   // flattened, 32-aligned ray space
+    long long rays = 0;
+    unsigned long long* d_counter = nullptr;
+    TraceTuning tune;
+    BuildArgs dims{};
+};
+
+namespace {
+// Scene buffers can be reallocated by a later synchronous build; the device
+// scene table must then be refreshed before any trace reads it.
+rtg_status batch_upload_views(rtg_batch b, cudaStream_t st, bool force) {
+    bool changed = force;
+    for (size_t i = 0; i < b->scenes.size(); ++i) {
+        BatchScene v;
+        v.view = view(b->scenes[i]);
+        if (std::memcmp(&v, &b->h_scenes[i], sizeof(BatchScene)) != 0) {
+            b->h_scenes[i] = v;
+            changed = true;
+        }
+    }
+    if (!changed) return RTG_OK;
+    CUDA_TRY(cudaMemcpyAsync(b->d_scenes, b->h_scenes.data(), sizeof(BatchScene) * b->h_scenes.size(),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+rtg_status batch_upload_build(rtg_batch b, cudaStream_t st, bool force) {
+    bool changed = force;
+    for (size_t i = 0; i < b->scenes.size(); ++i) {
+        BuildArgs a = make_args(b->scenes[i], b->k[i], false);
+        if (std::memcmp(&a, &b->h_build[i], sizeof(BuildArgs)) != 0) {
+            b->h_build[i] = a;
+            changed = true;
+        }
+    }
+    if (!changed) return RTG_OK;
+    BuildArgs dims{};
+    dims = b->h_build[0];
+    for (const BuildArgs& a : b->h_build) {
+        dims.nverts = a.nverts > dims.nverts ? a.nverts : dims.nverts;
+        dims.ntris = a.ntris > dims.ntris ? a.ntris : dims.ntris;
+        dims.cell_cap = a.cell_cap > dims.cell_cap ? a.cell_cap : dims.cell_cap;
+    }
+    dims.skip_bbox = false;
+    b->dims = dims;
+    CUDA_TRY(cudaMemcpyAsync(b->d_build, b->h_build.data(), sizeof(BuildArgs) * b->h_build.size(),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));   // the host copy may change before the next upload
+    return RTG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+rtg_status rtg_batch_create(const rtg_scene* scenes, int32_t nscenes, const int32_t* k, const rtg_trace_task* tasks,
+                            int32_t ntasks, rtg_batch* out) {
+    if (!out) return fail(RTG_INVALID_PARAM, "out is NULL");
+    *out = nullptr;
+    if (!scenes || nscenes <= 0 || nscenes > kMaxBatchScenes || !k || ntasks < 0 || (ntasks && !tasks))
+        return fail(RTG_INVALID_PARAM, "bad batch arguments (1..64 scenes)");
+    const int dev = scenes[0] ? scenes[0]->device : -1;
+    for (int i = 0; i < nscenes; ++i) {
+        if (!scenes[i] || scenes[i]->device != dev) return fail(RTG_INVALID_PARAM, "scenes must share one device");
+        if (scenes[i]->ntris == 0 || scenes[i]->nverts == 0) return fail(RTG_INVALID_PARAM, "empty scene in batch");
+        if (k[i] <= 0) return fail(RTG_INVALID_PARAM, "k must be positive");
+    }
+    for (int t = 0; t < ntasks; ++t) {
+        const rtg_trace_task& T = tasks[t];
+        if (T.scene < 0 || T.scene >= nscenes || T.n < 0 || (T.n && (!T.d_rays || !T.d_out)) ||
+            (T.mode != RTG_MODE_NEAREST && T.mode != RTG_MODE_ANY))
+            return fail(RTG_INVALID_PARAM, "bad trace task");
+    }
+    CUDA_TRY(cudaSetDevice(dev));
+    for (int i = 0; i < nscenes; ++i) {   // size every scene's buffers for its grid
+        rtg_status rc = rtg_scene_build(scenes[i], k[i], nullptr);
+        if (rc) return rc;
+    }
+    rtg_batch b = new rtg_batch_s();
+    b->device = dev;
+    b->num_sms = scenes[0]->num_sms;
+    b->scenes.assign(scenes, scenes + nscenes);
+    b->k.assign(k, k + nscenes);
+    b->h_build.resize(nscenes);
+    b->h_scenes.resize(nscenes);
+    std::vector<BatchTask> ht;
+    long long first = 0;
+    for (int t = 0; t < ntasks; ++t) {
+        if (tasks[t].n == 0) continue;
+        BatchTask T;
+        T.first = first;
+        T.n = tasks[t].n;
+        T.rays = reinterpret_cast<const float4*>(tasks[t].d_rays);
+        T.out = tasks[t].d_out;
+        T.scene = tasks[t].scene;
+        T.mode = tasks[t].mode;
+        ht.push_back(T);
+        first += (T.n + 31) / 32 * 32;
+        b->rays += T.n;
+    }
+    b->ntasks = (int)ht.size();
+    b->total = first;
+    rtg_status rc = RTG_OK;
+    if (cudaMalloc(&b->d_build, sizeof(BuildArgs) * nscenes) != cudaSuccess ||
+        cudaMalloc(&b->d_scenes, sizeof(BatchScene) * nscenes) != cudaSuccess ||
+        cudaMalloc(&b->d_tasks, sizeof(BatchTask) * (ht.size() + 1)) != cudaSuccess ||
+        cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess)
+        rc = fail(RTG_NO_MEMORY, "batch tables");
+    if (rc == RTG_OK && ht.size() &&
+        cudaMemcpy(b->d_tasks, ht.data(), sizeof(BatchTask) * ht.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = fail(RTG_DEVICE_ERROR, "batch table upload");
+    if (rc == RTG_OK) rc = batch_upload_views(b, scenes[0]->stream, true);
+    if (rc == RTG_OK) rc = batch_upload_build(b, scenes[0]->stream, true);
+    if (rc != RTG_OK) {
+        rtg_batch_destroy(b);
+        return rc;
+    }
+    *out = b;
+    return RTG_OK;
+}
+
+rtg_status rtg_batch_build_async(rtg_batch b, void* stream) {
+    if (!b) return fail(RTG_INVALID_PARAM, "batch is NULL");
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->scenes[0]->stream;
+    rtg_status rc = batch_upload_build(b, st, false);
+    if (rc == RTG_OK) rc = batch_upload_views(b, st, false);
+    if (rc) return rc;
+    launch_build_batch(b->d_build, (int)b->scenes.size(), b->dims, st);
+    CUDA_TRY(cudaGetLastError());
+    for (rtg_scene sc : b->scenes) sc->built = true;   // device status guards the traces
+    return RTG_OK;
+}
+
+rtg_status rtg_batch_trace_async(rtg_batch b, void* stream) {
+    if (!b) return fail(RTG_INVALID_PARAM, "batch is NULL");
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->scenes[0]->stream;
+    rtg_status rc = batch_upload_views(b, st, false);
+    if (rc) return rc;
+    launch_trace_batch(b->d_scenes, (int)b->scenes.size(), b->d_tasks, b->ntasks, b->total, b->d_counter, b->tune,
+                       b->num_sms, st);
+    CUDA_TRY(cudaGetLastError());
+    return RTG_OK;
+}
+
+rtg_status rtg_batch_check(rtg_batch b, void* stream) {
+    if (!b) return fail(RTG_INVALID_PARAM, "batch is NULL");
+    CUDA_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->scenes[0]->stream;
+    CUDA_TRY(cudaStreamSynchronize(st));
+    rtg_status worst = RTG_OK;
+    for (rtg_scene sc : b->scenes) {
+        rtg_status rc = rtg_scene_build_check(sc, nullptr);
+        if (rc != RTG_OK && worst == RTG_OK) worst = rc;
+    }
+    return worst;
+}
+
+rtg_status rtg_batch_rays(rtg_batch b, int64_t* rays) {
+    if (!b || !rays) return fail(RTG_INVALID_PARAM, "NULL argument");
+    *rays = b->rays;
+    return RTG_OK;
+}
+
+rtg_status rtg_batch_set_tuning(rtg_batch b, int32_t key, int32_t value) {
+    if (!b) return fail(RTG_INVALID_PARAM, "batch is NULL");
+    if (key == RTG_TUNE_EMPTY_RUN) {
+        if (value != 4 && value != 8 && value != 16) return fail(RTG_INVALID_PARAM, "empty run must be 4, 8 or 16");
+        b->tune.empty_run = value;
+        return RTG_OK;
+    }
+    if (key == RTG_TUNE_PERSISTENT) {
+        b->tune.persistent = value ? 1 : 0;
+        return RTG_OK;
+    }
+    return fail(RTG_INVALID_PARAM, "unknown tuning key");
+}
+
+rtg_status rtg_batch_destroy(rtg_batch b) {
+    if (!b) return RTG_OK;
+    cudaSetDevice(b->device);
+    cudaDeviceSynchronize();
+    cudaFree(b->d_build);
+    cudaFree(b->d_scenes);
+    cudaFree(b->d_tasks);
+    cudaFree(b->d_counter);
+    delete b;
+    return RTG_OK;
+}
+
+rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    switch (key) {
+        case RTG_TUNE_EMPTY_RUN:
+            if (value != 4 && value != 8 && value != 16) return fail(RTG_INVALID_PARAM, "empty run must be 4, 8 or 16");
+            s->tune.empty_run = value;
+            return RTG_OK;
+        case RTG_TUNE_PERSISTENT:
+            s->tune.persistent = value ? 1 : 0;
+            return RTG_OK;
+        default:
+            return fail(RTG_INVALID_PARAM, "unknown tuning key");
+    }
+}
 
 rtg_status rtg_scene_counters(rtg_scene s, int64_t out[3], int reset) {
     if (!s || !out) return fail(RTG_INVALID_PARAM, "NULL argument");

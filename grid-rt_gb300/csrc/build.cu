@@ -34,7 +34,7 @@ static constexpr unsigned FULL = 0xffffffffu;
 // ---------------------------------------------------------------------------
 // Aabb::buildFrom / expandBy (src/rtcore/Aabb.cpp:11-53): min/max per axis.
 // A NaN coordinate never wins a comparison there, so it is skipped here too.
-__global__ void __launch_bounds__(256) bbox_params_kernel(const float* __restrict__ verts, int64_t nverts,
+__device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts, int64_t nverts,
                                                           BuildWork* w, GridParams* p, int32_t k, int64_t ntris,
                                                           int64_t cell_cap) {
     float mn0 = INFINITY, mn1 = INFINITY, mn2 = INFINITY;
@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(256) bbox_params_kernel(const float* __restric
         p->inv[d] = frcp(cs);
     }
     if (ncells >= INT32_MAX) status |= ST_TOO_BIG;
+    // the occupancy bitmap shares the offsets capacity: words <= cells
     if (ncells + 1 > cell_cap) status |= ST_CELL_CAP;
     p->k = k;
     p->ncells = ncells;
@@ -143,12 +144,25 @@ __global__ void __launch_bounds__(256) bbox_params_kernel(const float* __restric
     if (status) atomicOr(&w->sticky, status);
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(256) bbox_params_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap);
+}
+
 static __device__ __forceinline__ bool fatal(uint32_t s) {
     return (s & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG)) != 0;
 }
 
-__global__ void zero_offsets_kernel(int32_t* __restrict__ offsets, const GridParams* __restrict__ p) {
+__device__ __forceinline__ void zero_offsets_body(int32_t* __restrict__ offsets, uint32_t* __restrict__ occ,
+                                    const GridParams* __restrict__ p) {
     if (fatal(p->status)) return;
+    if (occ) {
+        const int64_t words = occ_words(p->res[0], p->res[1], p->res[2]);
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words;
+             i += (int64_t)gridDim.x * blockDim.x)
+            occ[i] = 0u;
+    }
     const int64_t n = p->ncells + 1;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {
@@ -158,6 +172,12 @@ __global__ void zero_offsets_kernel(int32_t* __restrict__ offsets, const GridPar
             for (int64_t j = i; j < n && j < i + 4; ++j) offsets[j] = 0;
         }
     }
+}
+
+template <bool MULTI>
+__global__ void zero_offsets_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    zero_offsets_body(a.offsets, a.occ, a.params);
 }
 
 // ---------------------------------------------------------------------------
@@ -267,7 +287,7 @@ __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restri
     if (lane == 0 && total) atomicAdd(reinterpret_cast<unsigned long long*>(&p->nrefs), total);
 }
 
-__global__ void __launch_bounds__(256) count_kernel(const float* __restrict__ verts, const int32_t* __restrict__ idx,
+__device__ __forceinline__ void count_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
                                                     int64_t ntris, GridParams* p, BuildWork* w,
                                                     int32_t* __restrict__ counts, float4* __restrict__ tris) {
     if (fatal(p->status)) return;
@@ -285,7 +305,13 @@ __global__ void __launch_bounds__(256) count_kernel(const float* __restrict__ ve
     }
 }
 
-__global__ void __launch_bounds__(256) scatter_kernel(const float* __restrict__ verts, const int32_t* __restrict__ idx,
+template <bool MULTI>
+__global__ void __launch_bounds__(256) count_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris);
+}
+
+__device__ __forceinline__ void scatter_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
                                                       int64_t ntris, GridParams* p, int32_t* __restrict__ cursor,
                                                       int32_t* __restrict__ ids) {
     if (p->status & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP)) return;
@@ -353,6 +379,12 @@ __global__ void __launch_bounds__(256) scatter_kernel(const float* __restrict__ 
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    scatter_body(a.verts, a.idx, a.ntris, a.params, a.offsets, a.ids);
+}
+
 // ---------------------------------------------------------------------------
 // scan of the per-cell counts (in place, inclusive), three phases
 // ---------------------------------------------------------------------------
@@ -376,7 +408,7 @@ __device__ __forceinline__ int64_t block_sum_i64(int64_t v, int64_t* sh) {
     return s;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const int32_t* __restrict__ counts,
+__device__ __forceinline__ void scan_reduce_body(const int32_t* __restrict__ counts,
                                                                    const GridParams* __restrict__ p,
                                                                    int64_t* __restrict__ tile_sums) {
     if (fatal(p->status)) return;
@@ -394,7 +426,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const int32_t
     }
 }
 
-__global__ void __launch_bounds__(1024) scan_tiles_kernel(GridParams* p, BuildWork* w, int64_t* __restrict__ tile_sums,
+template <bool MULTI>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    scan_reduce_body(a.offsets, a.params, a.tile_sums);
+}
+
+__device__ __forceinline__ void scan_tiles_body(GridParams* p, BuildWork* w, int64_t* __restrict__ tile_sums,
                                                           int32_t* __restrict__ offsets, int64_t ref_cap) {
     if (fatal(p->status)) return;
     const int64_t C = p->ncells;
@@ -438,10 +476,17 @@ __global__ void __launch_bounds__(1024) scan_tiles_kernel(GridParams* p, BuildWo
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(1024) scan_tiles_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    scan_tiles_body(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap);
+}
+
 // In-place inclusive scan of each tile plus its prefix; queues cells that
 // hold two or more triangles for the segmented sort.
-__global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(int32_t* __restrict__ counts, GridParams* p,
+__device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, GridParams* p,
                                                                  const int64_t* __restrict__ tile_prefix,
+                                                                 uint32_t* __restrict__ occ,
                                                                  BuildWork* w, int32_t* __restrict__ q_small,
                                                                  int32_t* __restrict__ q_med,
                                                                  int32_t* __restrict__ q_large, int64_t q_small_cap,
@@ -478,6 +523,33 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(int32_t* __rest
         __syncthreads();
         int64_t run = tile_prefix[tile] + sh[wid] + x - s;
         __syncthreads();
+        if (occ && s > 0 && b < C) {
+            // occupancy bits of this thread's 16 consecutive cells (one row
+            // segment along x), one atomicOr per touched brick word
+            const int32_t nx = p->res[0], ny = p->res[1];
+            const int32_t bx = (nx + 3) >> 2, by = (ny + 3) >> 2;
+            int32_t cx = (int32_t)(b % nx);
+            const int64_t rest = b / nx;
+            int32_t cy = (int32_t)(rest % ny), cz = (int32_t)(rest / ny);
+            int64_t word = -1;
+            uint32_t mask = 0u;
+            for (int i = 0; i < SCAN_ITEMS && b + i < C; ++i) {
+                if (v[i] > 0) {
+                    const int64_t wi = (int64_t)(cx >> 2) + (int64_t)(cy >> 2) * bx + (int64_t)(cz >> 1) * bx * by;
+                    if (wi != word) {
+                        if (mask) atomicOr(&occ[word], mask);
+                        word = wi;
+                        mask = 0u;
+                    }
+                    mask |= occ_bit(cx, cy, cz);
+                }
+                if (++cx == nx) {
+                    cx = 0;
+                    if (++cy == ny) { cy = 0; ++cz; }
+                }
+            }
+            if (mask) atomicOr(&occ[word], mask);
+        }
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             if (b + i < C) {
@@ -504,6 +576,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(int32_t* __rest
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    scan_down_body(a.offsets, a.params, a.tile_sums, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap);
+}
+
 // ---------------------------------------------------------------------------
 // per-cell sorts (after scatter, offsets[c] .. offsets[c+1] is cell c's list)
 // ---------------------------------------------------------------------------
@@ -511,7 +589,7 @@ static __device__ __forceinline__ bool sort_skip(const GridParams* p) {
     return (p->status & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP | ST_SORT_CAP)) != 0;
 }
 
-__global__ void __launch_bounds__(256) sort_small_kernel(const int32_t* __restrict__ offsets, int32_t* __restrict__ ids,
+__device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offsets, int32_t* __restrict__ ids,
                                                          const int32_t* __restrict__ q, const BuildWork* w,
                                                          const GridParams* p) {
     if (sort_skip(p)) return;
@@ -537,9 +615,15 @@ __global__ void __launch_bounds__(256) sort_small_kernel(const int32_t* __restri
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    sort_small_body(a.offsets, a.ids, a.q_small, a.work, a.params);
+}
+
 static constexpr int MED_MAX = 4096;
 
-__global__ void __launch_bounds__(512) sort_medium_kernel(const int32_t* __restrict__ offsets,
+__device__ __forceinline__ void sort_medium_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, const int32_t* __restrict__ q,
                                                           const BuildWork* w, const GridParams* p) {
     if (sort_skip(p)) return;
@@ -570,9 +654,15 @@ __global__ void __launch_bounds__(512) sort_medium_kernel(const int32_t* __restr
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    sort_medium_body(a.offsets, a.ids, a.q_med, a.work, a.params);
+}
+
 // Cells above 4096 entries: copy the list to scratch, then per id chunk set
 // one shared-memory bit per id and write the set bits back in order.
-__global__ void __launch_bounds__(1024) sort_large_kernel(const int32_t* __restrict__ offsets,
+__device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, int32_t* __restrict__ scratch,
                                                           const int32_t* __restrict__ q, const BuildWork* w,
                                                           const GridParams* p, int32_t bitmap_words) {
@@ -650,41 +740,62 @@ __global__ void __launch_bounds__(1024) sort_large_kernel(const int32_t* __restr
     }
 }
 
+template <bool MULTI>
+__global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
+    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
+    sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words);
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_build(const BuildArgs& a, cudaStream_t st) {
-    const int sms = a.num_sms;
-    count_launches(a.skip_bbox ? 9 : 10);
-    if (!a.skip_bbox) {
-        int64_t blocks = (a.nverts + 255) / 256;
+// Enqueues the build.  Single scene: `one` is passed by value.  Batch:
+// `many` holds ntasks BuildArgs in device memory, block row y works on task y,
+// and `dims` carries the largest sizes over the tasks for the grid shapes.
+template <bool MULTI>
+static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BuildArgs& dims,
+                              cudaStream_t st) {
+    const int sms = dims.num_sms;
+    const unsigned ny = MULTI ? (unsigned)ntasks : 1u;
+    count_launches(dims.skip_bbox ? 9 : 10);
+    if (!dims.skip_bbox) {
+        int64_t blocks = (dims.nverts + 255) / 256;
         blocks = blocks < 1 ? 1 : (blocks > 2 * sms ? 2 * sms : blocks);
-        bbox_params_kernel<<<(int)blocks, 256, 0, st>>>(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap);
+        bbox_params_kernel<MULTI><<<dim3((unsigned)blocks, ny), 256, 0, st>>>(one, many);
     }
     {
-        int64_t blocks = (a.cell_cap / 4 + 255) / 256;
+        int64_t blocks = (dims.cell_cap / 4 + 255) / 256;
         blocks = blocks < 1 ? 1 : (blocks > 8 * sms ? 8 * sms : blocks);
-        zero_offsets_kernel<<<(int)blocks, 256, 0, st>>>(a.offsets, a.params);
+        zero_offsets_kernel<MULTI><<<dim3((unsigned)blocks, ny), 256, 0, st>>>(one, many);
     }
-    int64_t tri_blocks = (a.ntris + 255) / 256;   // one warp per 32 triangles
+    int64_t tri_blocks = (dims.ntris + 255) / 256;   // one warp per 32 triangles
     tri_blocks = tri_blocks < 1 ? 1 : (tri_blocks > 16 * sms ? 16 * sms : tri_blocks);
-    count_kernel<<<(int)tri_blocks, 256, 0, st>>>(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris);
-    int64_t tiles = (a.cell_cap + SCAN_TILE - 1) / SCAN_TILE;
+    count_kernel<MULTI><<<dim3((unsigned)tri_blocks, ny), 256, 0, st>>>(one, many);
+    int64_t tiles = (dims.cell_cap + SCAN_TILE - 1) / SCAN_TILE;
     tiles = tiles < 1 ? 1 : (tiles > 8 * sms ? 8 * sms : tiles);
-    scan_reduce_kernel<<<(int)tiles, SCAN_THREADS, 0, st>>>(a.offsets, a.params, a.tile_sums);
-    scan_tiles_kernel<<<1, 1024, 0, st>>>(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap);
-    scan_down_kernel<<<(int)tiles, SCAN_THREADS, 0, st>>>(a.offsets, a.params, a.tile_sums, a.work, a.q_small,
-                                                          a.q_med, a.q_large, a.q_small_cap, a.q_med_cap,
-                                                          a.q_large_cap);
-    scatter_kernel<<<(int)tri_blocks, 256, 0, st>>>(a.verts, a.idx, a.ntris, a.params, a.offsets, a.ids);
-    sort_small_kernel<<<8 * sms, 256, 0, st>>>(a.offsets, a.ids, a.q_small, a.work, a.params);
-    sort_medium_kernel<<<2 * sms, 512, 0, st>>>(a.offsets, a.ids, a.q_med, a.work, a.params);
-    sort_large_kernel<<<sms, 1024, (size_t)a.bitmap_words * 4, st>>>(a.offsets, a.ids, a.scratch, a.q_large, a.work,
-                                                                     a.params, a.bitmap_words);
+    scan_reduce_kernel<MULTI><<<dim3((unsigned)tiles, ny), SCAN_THREADS, 0, st>>>(one, many);
+    scan_tiles_kernel<MULTI><<<dim3(1, ny), 1024, 0, st>>>(one, many);
+    scan_down_kernel<MULTI><<<dim3((unsigned)tiles, ny), SCAN_THREADS, 0, st>>>(one, many);
+    scatter_kernel<MULTI><<<dim3((unsigned)tri_blocks, ny), 256, 0, st>>>(one, many);
+    const unsigned per_task = MULTI ? (unsigned)((sms + ntasks - 1) / ntasks) : (unsigned)sms;
+    sort_small_kernel<MULTI><<<dim3(8 * per_task, ny), 256, 0, st>>>(one, many);
+    sort_medium_kernel<MULTI><<<dim3(2 * per_task, ny), 512, 0, st>>>(one, many);
+    sort_large_kernel<MULTI><<<dim3(per_task, ny), 1024, (size_t)dims.bitmap_words * 4, st>>>(one, many);
+}
+
+void launch_build(const BuildArgs& a, cudaStream_t st) { launch_build_impl<false>(a, nullptr, 1, a, st); }
+
+void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BuildArgs& dims, cudaStream_t st) {
+    if (ntasks <= 0) return;
+    launch_build_impl<true>(dims, d_tasks, ntasks, dims, st);
 }
 
 cudaError_t build_setup_attributes(int bitmap_words) {
-    return cudaFuncSetAttribute(sort_large_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bitmap_words * 4);
+    cudaError_t e = cudaFuncSetAttribute(sort_large_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         bitmap_words * 4);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(sort_large_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                bitmap_words * 4);
 }
 
 }  // namespace gridrt

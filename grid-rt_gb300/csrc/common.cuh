@@ -83,6 +83,16 @@ __device__ __forceinline__ float voxel_to_world(int32_t vox, float cell, float b
     return fadd(fmul(__int2float_rn(vox), cell), bmin);
 }
 
+// Occupancy bitmap: one bit per cell, 32 cells per word grouped in 4x4x2
+// bricks so a DDA walk keeps using one word for several steps in any
+// direction.  Word count never exceeds the cell count.
+__host__ __device__ __forceinline__ int64_t occ_words(int32_t nx, int32_t ny, int32_t nz) {
+    return (int64_t)((nx + 3) >> 2) * ((ny + 3) >> 2) * ((nz + 1) >> 1);
+}
+__device__ __forceinline__ uint32_t occ_bit(int32_t x, int32_t y, int32_t z) {
+    return 1u << ((x & 3) | ((y & 3) << 2) | ((z & 1) << 4));
+}
+
 // Monotone float <-> uint32 key for atomicMin / atomicMax.
 __device__ __forceinline__ uint32_t f2key(float f) {
     uint32_t b = __float_as_uint(f);

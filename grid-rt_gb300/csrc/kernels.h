@@ -20,6 +20,7 @@ struct BuildArgs {
     BuildWork* work;
     float4* tris;          // 3 per triangle
     int32_t* offsets;      // cell_cap entries
+    uint32_t* occ;         // occupancy bitmap, cell_cap words (nullptr: not built)
     int64_t cell_cap;
     int32_t* ids;          // ref_cap entries
     int32_t* scratch;      // ref_cap entries
@@ -38,6 +39,10 @@ void count_launches(int n);
 unsigned long long launches_so_far();
 
 void launch_build(const BuildArgs& a, cudaStream_t st);
+// Batch: ntasks BuildArgs in device memory (block row y builds task y); dims
+// holds the largest nverts / ntris / cell_cap over the tasks plus num_sms and
+// bitmap_words.
+void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BuildArgs& dims, cudaStream_t st);
 // Host resolution of the grid parameters with the C library's powf (used when
 // the device flags ST_AMBIGUOUS); defined in api.cu.
 void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap);
@@ -50,6 +55,7 @@ struct SceneView {
     const GridParams* params;   // device
     const int32_t* offsets;
     const int32_t* ids;
+    const uint32_t* occ;
     const float4* tris;
 };
 
@@ -63,12 +69,38 @@ struct TraceCounters {
     unsigned long long rays, cells, tests;
 };
 
+// Trace launch shape, chosen per scene (rtg_scene_set_tuning / autotuner).
+struct TraceTuning {
+    int empty_run = 8;     // empty cells a lane may walk per loop iteration: 4, 8 or 16
+    int persistent = 1;    // 1: persistent warps over ray batches; 0: one batch per warp
+};
+
+// Trace launchers.  `counter` is a device word the launch zeroes and uses to
+// hand out ray batches; launches that may overlap need distinct counters.
 void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
-                          int num_sms, cudaStream_t st);
+                          unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st);
 void launch_trace_any(const SceneView& s, const float4* rays, int64_t n, uint8_t* occ, TraceCounters* ctr,
-                      int num_sms, cudaStream_t st);
+                      unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st);
 void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
-                         float4* shadow_rays, TraceCounters* ctr, int num_sms, cudaStream_t st);
+                         float4* shadow_rays, TraceCounters* ctr, unsigned long long* counter,
+                         const TraceTuning& tune, int num_sms, cudaStream_t st, int diffuse = 0,
+                         unsigned long long seed = 0);
+// Batched tracing: up to kMaxBatchScenes scenes, any number of tasks.
+static constexpr int kMaxBatchScenes = 64;
+struct BatchScene {
+    SceneView view;
+};
+struct BatchTask {
+    long long first;       // start of the task in the flattened, 32-aligned ray space
+    long long n;           // rays of the task
+    const float4* rays;    // n x 2 float4
+    void* out;             // int4 hits (closest) or uint8 occlusion (any)
+    int32_t scene;         // index into the scene table
+    int32_t mode;          // 0 closest, 1 any
+};
+void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
+                        unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st);
+
 void launch_deform(const float* base, const float* normals, float* out, int64_t nverts, float amp, float freq,
                    float phase, cudaStream_t st);
 

@@ -1,0 +1,63 @@
+// scene.h -- the scene object behind the rtg_scene handle (internal).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gridrt.h"
+#include "common.cuh"
+#include "kernels.h"
+
+struct rtg_scene_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+
+    float* d_verts = nullptr;
+    int64_t verts_cap = 0, nverts = 0;   // capacity in floats
+    int32_t* d_idx = nullptr;
+    int64_t idx_cap = 0, ntris = 0;      // capacity in ints
+    float4* d_tris = nullptr;
+    int64_t tris_cap = 0;                // float4 records
+
+    gridrt::GridParams* d_params = nullptr;
+    gridrt::GridParams* h_params = nullptr;      // pinned mirror
+    gridrt::BuildWork* d_work = nullptr;
+    int32_t* d_offsets = nullptr;
+    int64_t cell_cap = 0;
+    uint32_t* d_occ = nullptr;
+    int64_t occ_cap = 0;
+    unsigned long long* d_ray_ctr = nullptr;   // ring of per-launch ray counters
+    unsigned ctr_seq = 0;
+    gridrt::TraceTuning tune;
+    int32_t* d_ids = nullptr;
+    int64_t ids_cap = 0;
+    int32_t* d_scratch = nullptr;
+    int64_t scratch_cap = 0;
+    int64_t* d_tiles = nullptr;
+    int64_t tiles_cap = 0;
+    int32_t* d_qs = nullptr;
+    int64_t qs_cap = 0;
+    int32_t* d_qm = nullptr;
+    int64_t qm_cap = 0;
+    int32_t* d_ql = nullptr;
+    int64_t ql_cap = 0;
+    int32_t bitmap_words = 32768;
+
+    bool built = false;
+    int32_t k = 0;
+    gridrt::GridParams hp{};   // host copy of the last successful build
+
+    unsigned char* d_io = nullptr;
+    int64_t io_cap = 0;
+    gridrt::TraceCounters* d_ctr = nullptr;
+};
+
+namespace gridrt {
+constexpr unsigned kRayCounters = 64;
+// Read-only device view of a built scene (for the trace kernels).
+SceneView scene_view(rtg_scene s);
+// Next per-launch ray hand-out counter of the scene.
+unsigned long long* scene_counter(rtg_scene s);
+}  // namespace gridrt

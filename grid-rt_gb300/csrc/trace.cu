@@ -12,6 +12,14 @@
 // triangles are the reference's.  Only the triangle test differs (MT instead
 // of Wald's projection test), which moves t / u / v by a few ulps and can flip
 // the winner between triangles whose t differ by less than that (near-ties).
+//
+// Execution: persistent warps.  A warp claims 32 consecutive rays with one
+// global atomicAdd, traces them to the end (one ray per lane; consecutive
+// camera rays in Morton order stay coherent) and claims the next 32, so no
+// warp idles while a block-mate finishes.  Per loop iteration a lane walks up
+// to ER empty cells (a tuning parameter), decided from a 4x4x2-brick occupancy bitmap whose
+// current word stays in a register, and tests at most one non-empty cell, so
+// lanes that reach triangles test them together.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -23,13 +31,16 @@ static unsigned long long g_launches = 0;
 void count_launches(int n) { __atomic_add_fetch(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
 unsigned long long launches_so_far() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
-struct PLite {
+enum Mode : int { MODE_NEAREST = 0, MODE_ANY = 1, MODE_CAMERA = 2 };
+
+struct SParams {
     float bmin[3], bmax[3], cell[3], inv[3];
     int32_t res[3];
-    int32_t pad;
+    int32_t bx, bxby;
+    int32_t failed;
 };
 
-__device__ __forceinline__ void load_params(const GridParams* __restrict__ gp, PLite& P) {
+__device__ __forceinline__ void fill_sparams(const GridParams* __restrict__ gp, SParams& P) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         P.bmin[d] = gp->bmin[d];
@@ -38,13 +49,181 @@ __device__ __forceinline__ void load_params(const GridParams* __restrict__ gp, P
         P.inv[d] = gp->inv[d];
         P.res[d] = gp->res[d];
     }
+    P.bx = (P.res[0] + 3) >> 2;
+    P.bxby = P.bx * ((P.res[1] + 3) >> 2);
+    P.failed = build_failed(gp->status) ? 1 : 0;
 }
 
-struct TraceResult {
+__device__ __forceinline__ void load_sparams(const GridParams* __restrict__ gp, SParams& P) {
+    if (threadIdx.x == 0) fill_sparams(gp, P);
+    __syncthreads();
+}
+
+// Live state of one ray (registers).
+struct Lane {
+    float ox, oy, oz, dx, dy, dz;
+    float ix, iy, iz;
+    float tnear, tmax, lo;
+    float tMx, tMy, tMz, tDx, tDy, tDz;
+    int32_t x, y, z;
+    int32_t sx, sy, sz;      // steps (vr::sign of the direction)
+    int32_t ox_, oy_, oz_;   // out-of-grid limits (-1 or n)
+    int32_t budget;
+    float best;
     int32_t id;
-    float t, u, v;
-    uint32_t cells, tests;
+    int32_t cw;          // cached occupancy word index
+    uint32_t cword;      // its value
+    long long ray;       // ray index, -1 = none
 };
+
+// Ray::update + AabbIntersection::clipRay + traverse3ddda set-up
+// (include/rt/Ray.h:26-37, src/rtcore/AabbIntersection.cpp:37-63,
+//  src/rtplugins/UniformGridAccStruct.cpp:122-149).  False if the ray misses
+// the grid box.
+__device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear, float tfar) {
+    L.ix = frcp(L.dx);
+    L.iy = frcp(L.dy);
+    L.iz = frcp(L.dz);
+    L.tmax = tfar;
+    float rn = tnear, rf = tfar;
+    {
+        float tn = fmul(fsub(P.bmin[0], L.ox), L.ix), tf = fmul(fsub(P.bmax[0], L.ox), L.ix);
+        rn = vmax(rn, vmin(tn, tf));
+        rf = vmin(rf, vmax(tn, tf));
+        tn = fmul(fsub(P.bmin[1], L.oy), L.iy);
+        tf = fmul(fsub(P.bmax[1], L.oy), L.iy);
+        rn = vmax(rn, vmin(tn, tf));
+        rf = vmin(rf, vmax(tn, tf));
+        tn = fmul(fsub(P.bmin[2], L.oz), L.iz);
+        tf = fmul(fsub(P.bmax[2], L.oz), L.iz);
+        rn = vmax(rn, vmin(tn, tf));
+        rf = vmin(rf, vmax(tn, tf));
+    }
+    if (rn > rf) return false;
+    L.tnear = rn;
+    L.lo = fsub(rn, kHitEpsilon);
+    const int32_t sx = __float_as_uint(L.dx) >> 31, sy = __float_as_uint(L.dy) >> 31, sz = __float_as_uint(L.dz) >> 31;
+    L.x = vclamp(world_to_voxel(fadd(L.ox, fmul(L.dx, rn)), P.bmin[0], P.inv[0]), 0, P.res[0] - 1);
+    L.y = vclamp(world_to_voxel(fadd(L.oy, fmul(L.dy, rn)), P.bmin[1], P.inv[1]), 0, P.res[1] - 1);
+    L.z = vclamp(world_to_voxel(fadd(L.oz, fmul(L.dz, rn)), P.bmin[2], P.inv[2]), 0, P.res[2] - 1);
+    L.tDx = vabs(fmul(P.cell[0], L.ix));
+    L.tDy = vabs(fmul(P.cell[1], L.iy));
+    L.tDz = vabs(fmul(P.cell[2], L.iz));
+    L.tMx = fmul(fsub(voxel_to_world(L.x + (sx ^ 1), P.cell[0], P.bmin[0]), L.ox), L.ix);
+    L.tMy = fmul(fsub(voxel_to_world(L.y + (sy ^ 1), P.cell[1], P.bmin[1]), L.oy), L.iy);
+    L.tMz = fmul(fsub(voxel_to_world(L.z + (sz ^ 1), P.cell[2], P.bmin[2]), L.oz), L.iz);
+    L.sx = L.dx < 0.0f ? -1 : (L.dx > 0.0f ? 1 : 0);
+    L.sy = L.dy < 0.0f ? -1 : (L.dy > 0.0f ? 1 : 0);
+    L.sz = L.dz < 0.0f ? -1 : (L.dz > 0.0f ? 1 : 0);
+    L.ox_ = sx ? -1 : P.res[0];
+    L.oy_ = sy ? -1 : P.res[1];
+    L.oz_ = sz ? -1 : P.res[2];
+    // A walk visits at most nx+ny+nz-2 cells; the bound only guards against a
+    // zero direction component (outside the reference's domain) looping.
+    L.budget = P.res[0] + P.res[1] + P.res[2] + 3;
+    L.best = kFltMax;
+    L.id = -1;
+    L.cw = -1;
+    return true;
+}
+
+// One DDA step (src/rtplugins/UniformGridAccStruct.cpp:179-195): the strict-<
+// axis choice, then the exit test x != outX && y != outY && z != outZ with
+// out = -1 for a negative direction sign bit, n otherwise (:137-139).  True
+// when the walk has left the grid.
+__device__ __forceinline__ bool dda_step(const SParams& P, Lane& L) {
+    if (L.tMx < L.tMy && L.tMx < L.tMz) {
+        L.x += L.sx;
+        L.tMx = fadd(L.tMx, L.tDx);
+    } else if (L.tMy < L.tMz) {
+        L.y += L.sy;
+        L.tMy = fadd(L.tMy, L.tDy);
+    } else {
+        L.z += L.sz;
+        L.tMz = fadd(L.tMz, L.tDz);
+    }
+    return !(L.x != L.ox_ && L.y != L.oy_ && L.z != L.oz_) || --L.budget <= 0;
+}
+
+// Moller-Trumbore test of one triangle record against the lane's ray with the
+// reference's acceptance window.  Returns true when ANY mode found t < tmax.
+template <int MODE>
+__device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, const float4& B, const float4& C,
+                                         float hi) {
+    const float tvx = L.ox - A.x, tvy = L.oy - A.y, tvz = L.oz - A.z;
+    const float px = L.dy * C.z - L.dz * C.y;
+    const float py = L.dz * C.x - L.dx * C.z;
+    const float pz = L.dx * C.y - L.dy * C.x;
+    const float det = B.x * px + B.y * py + B.z * pz;
+    const float idet = frcp(det);
+    const float u = (tvx * px + tvy * py + tvz * pz) * idet;
+    const float qx = tvy * B.z - tvz * B.y;
+    const float qy = tvz * B.x - tvx * B.z;
+    const float qz = tvx * B.y - tvy * B.x;
+    const float v = (L.dx * qx + L.dy * qy + L.dz * qz) * idet;
+    const float t = (C.x * qx + C.y * qy + C.z * qz) * idet;
+    const bool acc = (t < L.best) && (t >= L.lo) && (t <= hi) && (u >= 0.0f) && (v >= 0.0f) &&
+                     ((1.0f - u) - v >= 0.0f);
+    if (acc) {
+        L.best = t;
+        L.id = tid;
+        if (MODE == MODE_ANY && t < L.tmax) return true;
+    }
+    return false;
+}
+
+// Visits up to ER empty cells and at most one non-empty cell.
+// Returns true when the ray is finished (hit decided, or left the grid).
+template <int MODE, int ER>
+__device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t* __restrict__ offsets,
+                                        const int32_t* __restrict__ ids, const float4* __restrict__ tris,
+                                        const uint32_t* __restrict__ occ, uint32_t& cells, uint32_t& tests) {
+    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
+    for (int s = 0; s < ER; ++s) {
+        ++cells;
+        const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+        if (w != L.cw) {
+            L.cw = w;
+            L.cword = __ldg(occ + w);
+        }
+        if (L.cword & occ_bit(L.x, L.y, L.z)) {
+            const int32_t c = L.x + L.y * nx + L.z * nxy;
+            const int32_t b = __ldg(offsets + c), e = __ldg(offsets + c + 1);
+            const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+            tests += (uint32_t)(e - b);
+            int32_t i = b;
+            for (; i + 1 < e; i += 2) {
+                const int32_t t0 = __ldg(ids + i), t1 = __ldg(ids + i + 1);
+                const float4 A0 = __ldg(tris + 3 * (int64_t)t0), B0 = __ldg(tris + 3 * (int64_t)t0 + 1),
+                             C0 = __ldg(tris + 3 * (int64_t)t0 + 2);
+                const float4 A1 = __ldg(tris + 3 * (int64_t)t1), B1 = __ldg(tris + 3 * (int64_t)t1 + 1),
+                             C1 = __ldg(tris + 3 * (int64_t)t1 + 2);
+                if (test_tri<MODE>(L, t0, A0, B0, C0, hi)) return true;
+                if (test_tri<MODE>(L, t1, A1, B1, C1, hi)) return true;
+            }
+            if (i < e) {
+                const int32_t t0 = __ldg(ids + i);
+                const float4 A0 = __ldg(tris + 3 * (int64_t)t0), B0 = __ldg(tris + 3 * (int64_t)t0 + 1),
+                             C0 = __ldg(tris + 3 * (int64_t)t0 + 2);
+                if (test_tri<MODE>(L, t0, A0, B0, C0, hi)) return true;
+            }
+            if (L.best < kFltMax) {
+                if (MODE == MODE_ANY) L.id = -1;   // first cell with a hit decides: not before tmax
+                return true;
+            }
+            if (dda_step(P, L)) {
+                L.id = -1;
+                return true;
+            }
+            return false;
+        }
+        if (dda_step(P, L)) {
+            L.id = -1;
+            return true;
+        }
+    }
+    return false;
+}
 
 // Reported hit values of the winning triangle.  Moller-Trumbore's u, v and t
 // come from dot products of the (large) origin-to-vertex vector, which cancel
@@ -52,151 +231,201 @@ struct TraceResult {
 // re-derived from the plane equation t = ((v0 - o).n) / (d.n) and u, v from
 // the hit point P = o + t*d projected on the triangle's dominant plane (the
 // quantities Wald's test evaluates, src/rtcore/RayTriIntersection.cpp:15-47).
-// The accept / reject decisions above stay Moller-Trumbore's.
-__device__ __forceinline__ void refine_hit(const float4* __restrict__ tris, TraceResult& R, const float o[3],
-                                           const float d[3]) {
-    const float4 A = __ldg(tris + 3 * (int64_t)R.id);
-    const float4 B = __ldg(tris + 3 * (int64_t)R.id + 1);
-    const float4 C = __ldg(tris + 3 * (int64_t)R.id + 2);
+// The accept / reject decisions stay Moller-Trumbore's.
+__device__ __forceinline__ int4 refined_hit(const float4* __restrict__ tris, const Lane& L) {
+    const float4 A = __ldg(tris + 3 * (int64_t)L.id);
+    const float4 B = __ldg(tris + 3 * (int64_t)L.id + 1);
+    const float4 C = __ldg(tris + 3 * (int64_t)L.id + 2);
     const float nx = B.y * C.z - B.z * C.y, ny = B.z * C.x - B.x * C.z, nz = B.x * C.y - B.y * C.x;
-    const float num = (A.x - o[0]) * nx + (A.y - o[1]) * ny + (A.z - o[2]) * nz;
-    const float den = d[0] * nx + d[1] * ny + d[2] * nz;
+    const float num = (A.x - L.ox) * nx + (A.y - L.oy) * ny + (A.z - L.oz) * nz;
+    const float den = L.dx * nx + L.dy * ny + L.dz * nz;
     const float t = num / den;
-    const float wx = (o[0] + t * d[0]) - A.x, wy = (o[1] + t * d[1]) - A.y, wz = (o[2] + t * d[2]) - A.z;
+    const float wx = (L.ox + t * L.dx) - A.x, wy = (L.oy + t * L.dy) - A.y, wz = (L.oz + t * L.dz) - A.z;
     const float ax = fabsf(nx), ay = fabsf(ny), az = fabsf(nz);
     float e1a, e1b, e2a, e2b, wa, wb;
-    if (ax > ay && ax > az) {          // drop x
+    if (ax > ay && ax > az) {
         e1a = B.y; e1b = B.z; e2a = C.y; e2b = C.z; wa = wy; wb = wz;
-    } else if (ay > az) {              // drop y
+    } else if (ay > az) {
         e1a = B.z; e1b = B.x; e2a = C.z; e2b = C.x; wa = wz; wb = wx;
-    } else {                           // drop z
+    } else {
         e1a = B.x; e1b = B.y; e2a = C.x; e2b = C.y; wa = wx; wb = wy;
     }
     const float D = e1a * e2b - e2a * e1b;
-    const float u = (wa * e2b - e2a * wb) / D;
-    const float v = (e1a * wb - wa * e1b) / D;
-    if (isfinite(t) && isfinite(u) && isfinite(v)) {
-        R.t = t;
-        R.u = u;
-        R.v = v;
+    float u = (wa * e2b - e2a * wb) / D;
+    float v = (e1a * wb - wa * e1b) / D;
+    float tt = t;
+    if (!(isfinite(t) && isfinite(u) && isfinite(v))) {
+        tt = L.best;   // degenerate refinement: keep the decision's t
+        u = 0.0f;
+        v = 0.0f;
+    }
+    return make_int4(L.id, __float_as_int(tt), __float_as_int(u), __float_as_int(v));
+}
+
+__device__ __forceinline__ void ray_pixel(long long i, const CameraArgs& cam, int32_t& px, int32_t& py) {
+    if (cam.order == 1) {
+        const long long tile = i >> 6;
+        const int32_t r = (int32_t)(i & 63);
+        const int32_t tiles_x = cam.width >> 3;
+        const int32_t tx = (int32_t)(tile % tiles_x), ty = (int32_t)(tile / tiles_x);
+        px = tx * 8 + ((r & 1) | ((r >> 1) & 2) | ((r >> 2) & 4));
+        py = ty * 8 + (((r >> 1) & 1) | ((r >> 2) & 2) | ((r >> 3) & 4));
+    } else {
+        px = (int32_t)(i % cam.width);
+        py = (int32_t)(i / cam.width);
     }
 }
 
-// ANY = false: closest hit.  ANY = true: returns id >= 0 iff occluded before tmax.
-template <bool ANY>
-__device__ __forceinline__ TraceResult traverse(const PLite& P, const int32_t* __restrict__ offsets,
-                                                const int32_t* __restrict__ ids, const float4* __restrict__ tris,
-                                                const float o[3], const float d[3], float tnear, float tfar) {
-    TraceResult R;
-    R.id = -1; R.t = 0.f; R.u = 0.f; R.v = 0.f; R.cells = 0; R.tests = 0;
-    const float tmax = tfar;
-    // Ray::update (include/rt/Ray.h:26-37)
-    float inv[3];
-    int32_t sgn[3], sbit[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        inv[a] = frcp(d[a]);
-        sgn[a] = d[a] < 0.0f ? -1 : (d[a] > 0.0f ? 1 : 0);
-        sbit[a] = (__float_as_uint(d[a]) >> 31);
-    }
-    // AabbIntersection::clipRay (src/rtcore/AabbIntersection.cpp:37-63)
-    float rn = tnear, rf = tfar;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float tn = fmul(fsub(P.bmin[a], o[a]), inv[a]);
-        const float tf = fmul(fsub(P.bmax[a], o[a]), inv[a]);
-        rn = vmax(rn, vmin(tn, tf));
-        rf = vmin(rf, vmax(tn, tf));
-    }
-    if (rn > rf) return R;
-    tnear = rn;
-    // traverse3ddda setup (src/rtplugins/UniformGridAccStruct.cpp:122-149)
-    const int32_t nx = P.res[0], ny = P.res[1], nz = P.res[2];
-    int32_t c3[3];
-    float tMax[3], tDelta[3];
-    int32_t out[3];
-    const int32_t nn[3] = {nx, ny, nz};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float sp = fadd(o[a], fmul(d[a], tnear));
-        c3[a] = vclamp(world_to_voxel(sp, P.bmin[a], P.inv[a]), 0, nn[a] - 1);
-        out[a] = -sbit[a] + nn[a] * (sbit[a] ^ 1);
-        tDelta[a] = vabs(fmul(P.cell[a], inv[a]));
-        tMax[a] = fmul(fsub(voxel_to_world(c3[a] + (sbit[a] ^ 1), P.cell[a], P.bmin[a]), o[a]), inv[a]);
-    }
-    int32_t x = c3[0], y = c3[1], z = c3[2];
-    float tMaxX = tMax[0], tMaxY = tMax[1], tMaxZ = tMax[2];
-    const float lo = fsub(tnear, kHitEpsilon);
-    const int32_t nxy = nx * ny;
-    // A DDA walk visits at most nx+ny+nz-2 cells; the bound only guards
-    // against non-finite rays (a zero direction component) looping forever.
-    int32_t budget = nx + ny + nz + 3;
-    float best = kFltMax;
-    do {
-        const int32_t c = x + y * nx + z * nxy;
-        const int32_t b = __ldg(offsets + c), e = __ldg(offsets + c + 1);
-        ++R.cells;
-        if (b != e) {
-            const float cell_exit = vmin(vmin(tMaxX, tMaxY), tMaxZ);
-            const float hi = fadd(cell_exit, kHitEpsilon);
-            R.tests += (uint32_t)(e - b);
-            for (int32_t i = b; i < e; ++i) {
-                const int32_t tid = __ldg(ids + i);
-                const float4 A = __ldg(tris + 3 * (int64_t)tid);
-                const float4 B = __ldg(tris + 3 * (int64_t)tid + 1);
-                const float4 C = __ldg(tris + 3 * (int64_t)tid + 2);
-                // Moller-Trumbore: v0 = A.xyz, e1 = B.xyz, e2 = C.xyz
-                const float tvx = o[0] - A.x, tvy = o[1] - A.y, tvz = o[2] - A.z;
-                const float px = d[1] * C.z - d[2] * C.y;
-                const float py = d[2] * C.x - d[0] * C.z;
-                const float pz = d[0] * C.y - d[1] * C.x;
-                const float det = B.x * px + B.y * py + B.z * pz;
-                const float idet = frcp(det);
-                const float u = (tvx * px + tvy * py + tvz * pz) * idet;
-                const float qx = tvy * B.z - tvz * B.y;
-                const float qy = tvz * B.x - tvx * B.z;
-                const float qz = tvx * B.y - tvy * B.x;
-                const float v = (d[0] * qx + d[1] * qy + d[2] * qz) * idet;
-                const float t = (C.x * qx + C.y * qy + C.z * qz) * idet;
-                const bool acc = (t < best) && (t >= lo) && (t <= hi) && (u >= 0.0f) && (v >= 0.0f) &&
-                                 ((1.0f - u) - v >= 0.0f);
-                if (acc) {
-                    if (ANY && t < tmax) {
-                        R.id = tid; R.t = t; R.u = u; R.v = v;
-                        return R;
-                    }
-                    best = t;
-                    R.id = tid; R.t = t; R.u = u; R.v = v;
-                }
-            }
-            if (best < kFltMax) {
-                if (ANY) {
-                    R.id = -1;   // first cell with a hit decides: not before tmax
-                } else {
-                    refine_hit(tris, R, o, d);
-                }
-                return R;
-            }
+struct TraceIO {
+    const float4* rays;       // NEAREST / ANY
+    int4* hits;               // NEAREST / CAMERA
+    uint8_t* occ;             // ANY
+    float4* shadow_rays;      // CAMERA (optional): shadow or diffuse secondary rays
+    CameraArgs cam;           // CAMERA
+    float3 light;
+    int has_light;
+    int diffuse;              // CAMERA: secondary = cosine-weighted diffuse ray
+    unsigned long long seed;
+    long long n;
+    unsigned long long* counter;
+    TraceCounters* ctr;
+};
+
+// Loads ray `r` into the lane; false when the ray ends at once (misses the
+// grid, or ANY mode with no shadow ray).
+template <int MODE>
+__device__ __forceinline__ bool start_ray(const SParams& P, const TraceIO& io, Lane& L, long long r) {
+    float tnear, tfar;
+    if (MODE == MODE_CAMERA) {
+        int32_t px, py;
+        ray_pixel(r, io.cam, px, py);
+        const float us = fmul(fadd(__int2float_rn(px), 0.5f), io.cam.inv_w);
+        const float vs = fmul(fadd(__int2float_rn(py), 0.5f), io.cam.inv_h);
+        L.ox = io.cam.eye[0]; L.oy = io.cam.eye[1]; L.oz = io.cam.eye[2];
+        L.dx = fadd(fadd(io.cam.base[0], fmul(io.cam.nu[0], us)), fmul(io.cam.nv[0], vs));
+        L.dy = fadd(fadd(io.cam.base[1], fmul(io.cam.nu[1], us)), fmul(io.cam.nv[1], vs));
+        L.dz = fadd(fadd(io.cam.base[2], fmul(io.cam.nu[2], us)), fmul(io.cam.nv[2], vs));
+        tnear = kRayEpsilon;
+        tfar = kFltMax;
+    } else {
+        const float4 a = __ldg(io.rays + 2 * r), b = __ldg(io.rays + 2 * r + 1);
+        L.ox = a.x; L.oy = a.y; L.oz = a.z;
+        L.dx = b.x; L.dy = b.y; L.dz = b.z;
+        tnear = a.w;
+        tfar = b.w;
+        if (MODE == MODE_ANY && tfar < 0.0f) {   // no shadow ray for this slot
+            L.id = -2;
+            return false;
         }
-        if (tMaxX < tMaxY && tMaxX < tMaxZ) {
-            x += sgn[0];
-            tMaxX = fadd(tMaxX, tDelta[0]);
-        } else if (tMaxY < tMaxZ) {
-            y += sgn[1];
-            tMaxY = fadd(tMaxY, tDelta[1]);
-        } else {
-            z += sgn[2];
-            tMaxZ = fadd(tMaxZ, tDelta[2]);
-        }
-    } while (x != out[0] && y != out[1] && z != out[2] && --budget > 0);
-    R.id = -1;
-    return R;
+    }
+    L.id = -1;
+    L.best = kFltMax;
+    if (P.failed) return false;
+    return setup_ray(P, L, tnear, tfar);
 }
 
-template <bool COUNT>
-__device__ __forceinline__ void add_counters(TraceCounters* ctr, uint32_t cells, uint32_t tests, bool valid) {
-    if (!COUNT) return;
-    unsigned long long r = valid ? 1 : 0, c = cells, t = tests;
+// splitmix64 finaliser: counter-based random bits for ray index `i`.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// Cosine-weighted direction about unit normal n (Malley's method: uniform
+// disc sample lifted to the hemisphere), 24-bit uniforms from mix64.
+__device__ __forceinline__ float3 cosine_dir(float nx, float ny, float nz, unsigned long long bits) {
+    const float u1 = (float)(bits >> 40) * (1.0f / 16777216.0f);
+    const float u2 = (float)((bits >> 16) & 0xffffffull) * (1.0f / 16777216.0f);
+    const float r = sqrtf(u1);
+    float sp, cp;
+    sincospif(2.0f * u2, &sp, &cp);
+    const float lx = r * cp, ly = r * sp, lz = sqrtf(fmaxf(0.0f, 1.0f - u1));
+    // orthonormal basis (Frisvad-style, branch on the sign of nz)
+    const float sgn = nz >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (sgn + nz);
+    const float b = nx * ny * a;
+    const float tx = 1.0f + sgn * nx * nx * a, ty = sgn * b, tz = -sgn * nx;
+    const float bx = b, by = sgn + ny * ny * a, bz = -ny;
+    return make_float3(lx * tx + ly * bx + lz * nx, lx * ty + ly * by + lz * ny, lx * tz + ly * bz + lz * nz);
+}
+
+template <int MODE>
+__device__ __forceinline__ void finish_ray(const TraceIO& io, const float4* __restrict__ tris, const Lane& L) {
+    const long long r = L.ray;
+    if (MODE == MODE_ANY) {
+        io.occ[r] = L.id == -2 ? 2 : (L.id >= 0 ? 1 : 0);
+        return;
+    }
+    int4 h = make_int4(-1, 0, 0, 0);
+    if (L.id >= 0) h = refined_hit(tris, L);
+    io.hits[r] = h;
+    if (MODE == MODE_CAMERA && io.shadow_rays) {
+        // Sample::computeHitPosition, flat normal facing the ray, initLightRay
+        // offset and initShadowRay (src/rtcore/Sample.cpp:22-42,177-180,224-236),
+        // SimplePointLight::illuminate (src/rtplugins/SimplePointLight.cpp:25-33)
+        float4 sa = make_float4(0.f, 0.f, 0.f, kRayEpsilon), sb = make_float4(0.f, 0.f, 0.f, -1.0f);
+        if (L.id >= 0 && io.diffuse) {
+            // secondary diffuse ray from the hit point, offset along the
+            // normal facing the incoming ray, tnear 2e-4, tfar FLT_MAX
+            const float t = __int_as_float(h.y);
+            const float4 B = __ldg(tris + 3 * (int64_t)L.id + 1);
+            const float4 C = __ldg(tris + 3 * (int64_t)L.id + 2);
+            float nx = B.y * C.z - B.z * C.y, ny = B.z * C.x - B.x * C.z, nz = B.x * C.y - B.y * C.x;
+            const float rl = rsqrtf(nx * nx + ny * ny + nz * nz);
+            nx *= rl; ny *= rl; nz *= rl;
+            if (nx * L.dx + ny * L.dy + nz * L.dz > 0.0f) { nx = -nx; ny = -ny; nz = -nz; }
+            const float3 w = cosine_dir(nx, ny, nz, mix64(io.seed ^ mix64((unsigned long long)r)));
+            sa = make_float4(L.ox + L.dx * t + nx * kRayEpsilon, L.oy + L.dy * t + ny * kRayEpsilon,
+                             L.oz + L.dz * t + nz * kRayEpsilon, kRayEpsilon);
+            sb = make_float4(w.x, w.y, w.z, kFltMax);
+        } else if (L.id >= 0 && io.has_light) {
+            const float t = __int_as_float(h.y);
+            const float4 B = __ldg(tris + 3 * (int64_t)L.id + 1);
+            const float4 C = __ldg(tris + 3 * (int64_t)L.id + 2);
+            float nx = B.y * C.z - B.z * C.y, ny = B.z * C.x - B.x * C.z, nz = B.x * C.y - B.y * C.x;
+            const float rl = rsqrtf(nx * nx + ny * ny + nz * nz);
+            nx *= rl; ny *= rl; nz *= rl;
+            if (nx * L.dx + ny * L.dy + nz * L.dz > 0.0f) { nx = -nx; ny = -ny; nz = -nz; }
+            const float hx = L.ox + L.dx * t + nx * kRayEpsilon;
+            const float hy = L.oy + L.dy * t + ny * kRayEpsilon;
+            const float hz = L.oz + L.dz * t + nz * kRayEpsilon;
+            const float lx = io.light.x - hx, ly = io.light.y - hy, lz = io.light.z - hz;
+            if (nx * lx + ny * ly + nz * lz > 0.0f) {
+                sa = make_float4(hx, hy, hz, kRayEpsilon);
+                sb = make_float4(lx, ly, lz, 1.0f);
+            }
+        }
+        io.shadow_rays[2 * r] = sa;
+        io.shadow_rays[2 * r + 1] = sb;
+    }
+}
+
+// Traces the 32 rays [base, base + 32) of `io` (one per lane) to the end.
+template <int MODE, int ER>
+__device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView& s, const TraceIO& io, Lane& L,
+                                              long long base, uint32_t& cells, uint32_t& tests, uint32_t& started) {
+    const int lane = threadIdx.x & 31;
+    L.ray = base + lane;
+    bool active = L.ray < io.n;
+    if (active) {
+        ++started;
+        if (!start_ray<MODE>(P, io, L, L.ray)) {
+            if (L.id != -2) L.id = -1;
+            finish_ray<MODE>(io, s.tris, L);
+            active = false;
+        }
+    }
+    while (__any_sync(FULL, active)) {
+        if (active && advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, cells, tests)) {
+            finish_ray<MODE>(io, s.tris, L);
+            active = false;
+        }
+    }
+}
+
+__device__ __forceinline__ void flush_counters(TraceCounters* ctr, uint32_t started, uint32_t cells, uint32_t tests) {
+    unsigned long long r = started, c = cells, t = tests;
     for (int o = 16; o > 0; o >>= 1) {
         r += __shfl_xor_sync(FULL, r, o);
         c += __shfl_xor_sync(FULL, c, o);
@@ -209,123 +438,61 @@ __device__ __forceinline__ void add_counters(TraceCounters* ctr, uint32_t cells,
     }
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(256) trace_nearest_kernel(SceneView s, const float4* __restrict__ rays, int64_t n,
-                                                            int4* __restrict__ hits, TraceCounters* ctr) {
-    PLite P;
-    load_params(s.params, P);
-    const bool failed = build_failed(s.params->status);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        TraceResult R;
-        R.cells = R.tests = 0;
-        if (i < n) {
-            const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
-            const float o[3] = {a.x, a.y, a.z}, d[3] = {b.x, b.y, b.z};
-            if (!failed) R = traverse<false>(P, s.offsets, s.ids, s.tris, o, d, a.w, b.w);
-            else R.id = -1;
-            hits[i] = make_int4(R.id, __float_as_int(R.t), __float_as_int(R.u), __float_as_int(R.v));
-        }
-        add_counters<COUNT>(ctr, R.cells, R.tests, i < n);
+template <int MODE, bool COUNT, int ER>
+__global__ void __launch_bounds__(128) trace_kernel(SceneView s, TraceIO io) {
+    __shared__ SParams P;
+    load_sparams(s.params, P);
+    const int lane = threadIdx.x & 31;
+    Lane L;
+    uint32_t cells = 0, tests = 0, started = 0;
+    for (;;) {
+        // the warp claims the next 32 consecutive rays and traces them to the end
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(io.counter, 32ull);
+        b = __shfl_sync(FULL, b, 0);
+        if ((long long)b >= io.n) break;
+        trace_batch32<MODE, ER>(P, s, io, L, (long long)b, cells, tests, started);
     }
+    if (COUNT) flush_counters(io.ctr, started, cells, tests);
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(256) trace_any_kernel(SceneView s, const float4* __restrict__ rays, int64_t n,
-                                                        uint8_t* __restrict__ occ, TraceCounters* ctr) {
-    PLite P;
-    load_params(s.params, P);
-    const bool failed = build_failed(s.params->status);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        TraceResult R;
-        R.cells = R.tests = 0;
-        bool valid = false;
-        if (i < n) {
-            const float4 a = __ldg(rays + 2 * i), b = __ldg(rays + 2 * i + 1);
-            uint8_t r = 2;   // no shadow ray (tmax < 0)
-            if (b.w >= 0.0f) {
-                const float o[3] = {a.x, a.y, a.z}, d[3] = {b.x, b.y, b.z};
-                if (!failed) R = traverse<true>(P, s.offsets, s.ids, s.tris, o, d, a.w, b.w);
-                else R.id = -1;
-                r = R.id >= 0 ? 1 : 0;
-                valid = true;
-            }
-            occ[i] = r;
+// Many (scene, ray batch) tasks in one persistent launch.  Task t owns the
+// 32-aligned index range [first, first + n) of one flattened ray space, so a
+// 32-ray claim always falls inside one task: scene and mode are warp-uniform.
+template <int ER>
+__global__ void __launch_bounds__(128) trace_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes,
+                                                          const BatchTask* __restrict__ tasks, int ntasks,
+                                                          long long total, unsigned long long* counter) {
+    __shared__ SParams P[kMaxBatchScenes];
+    for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    Lane L;
+    uint32_t cells = 0, tests = 0, started = 0;
+    for (;;) {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(counter, 32ull);
+        b = __shfl_sync(FULL, b, 0);
+        if ((long long)b >= total) break;
+        int lo = 0, hi = ntasks - 1;       // last task with first <= b
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tasks[mid].first <= (long long)b) lo = mid;
+            else hi = mid - 1;
         }
-        add_counters<COUNT>(ctr, R.cells, R.tests, valid);
-    }
-}
-
-__device__ __forceinline__ void ray_pixel(int64_t i, const CameraArgs& cam, int32_t& px, int32_t& py) {
-    if (cam.order == 1) {
-        const int64_t tile = i >> 6;
-        const int32_t r = (int32_t)(i & 63);
-        const int32_t tiles_x = cam.width >> 3;
-        const int32_t tx = (int32_t)(tile % tiles_x), ty = (int32_t)(tile / tiles_x);
-        px = tx * 8 + ((r & 1) | ((r >> 1) & 2) | ((r >> 2) & 4));
-        py = ty * 8 + (((r >> 1) & 1) | ((r >> 2) & 2) | ((r >> 3) & 4));
-    } else {
-        px = (int32_t)(i % cam.width);
-        py = (int32_t)(i / cam.width);
-    }
-}
-
-// Primary rays at pixel centres (PinholeCamera::getRayDirection,
-// src/rtplugins/PinholeCamera.cpp:131-137), then optionally the shadow ray of
-// SimplePointLight::illuminate (src/rtplugins/SimplePointLight.cpp:18-52).
-template <bool COUNT>
-__global__ void __launch_bounds__(256) trace_camera_kernel(SceneView s, CameraArgs cam, int4* __restrict__ hits,
-                                                           float3 light, int has_light,
-                                                           float4* __restrict__ shadow_rays, TraceCounters* ctr) {
-    PLite P;
-    load_params(s.params, P);
-    const bool failed = build_failed(s.params->status);
-    const int64_t n = (int64_t)cam.width * cam.height;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        TraceResult R;
-        R.cells = R.tests = 0;
-        if (i < n) {
-            int32_t px, py;
-            ray_pixel(i, cam, px, py);
-            const float us = fmul(fadd(__int2float_rn(px), 0.5f), cam.inv_w);
-            const float vs = fmul(fadd(__int2float_rn(py), 0.5f), cam.inv_h);
-            float d[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) d[a] = fadd(fadd(cam.base[a], fmul(cam.nu[a], us)), fmul(cam.nv[a], vs));
-            const float o[3] = {cam.eye[0], cam.eye[1], cam.eye[2]};
-            if (!failed) R = traverse<false>(P, s.offsets, s.ids, s.tris, o, d, kRayEpsilon, kFltMax);
-            else R.id = -1;
-            hits[i] = make_int4(R.id, __float_as_int(R.t), __float_as_int(R.u), __float_as_int(R.v));
-            if (shadow_rays) {
-                float4 sa = make_float4(0.f, 0.f, 0.f, kRayEpsilon), sb = make_float4(0.f, 0.f, 0.f, -1.0f);
-                if (R.id >= 0 && has_light) {
-                    // Sample::computeHitPosition, flat normal facing the ray,
-                    // initLightRay offset and initShadowRay (src/rtcore/Sample.cpp:22-42,177-180,224-236)
-                    const float4 B = __ldg(s.tris + 3 * (int64_t)R.id + 1);
-                    const float4 C = __ldg(s.tris + 3 * (int64_t)R.id + 2);
-                    float nx = B.y * C.z - B.z * C.y, ny = B.z * C.x - B.x * C.z, nz = B.x * C.y - B.y * C.x;
-                    const float rl = rsqrtf(nx * nx + ny * ny + nz * nz);
-                    nx *= rl; ny *= rl; nz *= rl;
-                    if (nx * d[0] + ny * d[1] + nz * d[2] > 0.0f) { nx = -nx; ny = -ny; nz = -nz; }
-                    const float hx = o[0] + d[0] * R.t + nx * kRayEpsilon;
-                    const float hy = o[1] + d[1] * R.t + ny * kRayEpsilon;
-                    const float hz = o[2] + d[2] * R.t + nz * kRayEpsilon;
-                    const float lx = light.x - hx, ly = light.y - hy, lz = light.z - hz;
-                    if (nx * lx + ny * ly + nz * lz > 0.0f) {
-                        sa = make_float4(hx, hy, hz, kRayEpsilon);
-                        sb = make_float4(lx, ly, lz, 1.0f);
-                    }
-                }
-                shadow_rays[2 * i] = sa;
-                shadow_rays[2 * i + 1] = sb;
-            }
+        const BatchTask T = tasks[lo];
+        const SceneView V = scenes[T.scene].view;
+        TraceIO io{};
+        io.rays = T.rays;
+        io.n = T.n;
+        const long long base = (long long)b - T.first;
+        if (T.mode == MODE_ANY) {
+            io.occ = static_cast<uint8_t*>(T.out);
+            trace_batch32<MODE_ANY, ER>(P[T.scene], V, io, L, base, cells, tests, started);
+        } else {
+            io.hits = static_cast<int4*>(T.out);
+            trace_batch32<MODE_NEAREST, ER>(P[T.scene], V, io, L, base, cells, tests, started);
         }
-        add_counters<COUNT>(ctr, R.cells, R.tests, i < n);
     }
 }
 
@@ -341,41 +508,107 @@ __global__ void deform_kernel(const float* __restrict__ base, const float* __res
     }
 }
 
-static int grid_for(int64_t n, int num_sms) {
-    int64_t blocks = (n + 255) / 256;
-    const int64_t cap = (int64_t)num_sms * 64;
-    if (blocks > cap) blocks = cap;
-    return (int)(blocks < 1 ? 1 : blocks);
+// Blocks of 128 threads.  Persistent: as many blocks as fit on the device at
+// once, warps loop over ray batches.  One-shot: one batch per warp, blocks
+// scheduled by the hardware.
+template <int MODE, bool COUNT, int ER>
+static void launch_er(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_kernel<MODE, COUNT, ER>, 128, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    long long blocks = (io.n + 127) / 128;
+    if (tune.persistent) blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
+    trace_kernel<MODE, COUNT, ER><<<(int)blocks, 128, 0, st>>>(s, io);
+}
+
+template <int MODE, bool COUNT>
+static void launch_count(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms,
+                         cudaStream_t st) {
+    if (tune.empty_run <= 4) launch_er<MODE, COUNT, 4>(s, io, tune, num_sms, st);
+    else if (tune.empty_run <= 8) launch_er<MODE, COUNT, 8>(s, io, tune, num_sms, st);
+    else launch_er<MODE, COUNT, 16>(s, io, tune, num_sms, st);
+}
+
+template <int MODE>
+static void launch_mode(const SceneView& s, TraceIO io, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+    count_launches(1);
+    cudaMemsetAsync(io.counter, 0, sizeof(unsigned long long), st);
+    if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
+    else launch_count<MODE, false>(s, io, tune, num_sms, st);
 }
 
 void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
-                          int num_sms, cudaStream_t st) {
+                          unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     if (n <= 0) return;
-    count_launches(1);
-    if (ctr) trace_nearest_kernel<true><<<grid_for(n, num_sms), 256, 0, st>>>(s, rays, n, hits, ctr);
-    else trace_nearest_kernel<false><<<grid_for(n, num_sms), 256, 0, st>>>(s, rays, n, hits, ctr);
+    TraceIO io{};
+    io.rays = rays;
+    io.hits = hits;
+    io.n = n;
+    io.counter = counter;
+    io.ctr = ctr;
+    launch_mode<MODE_NEAREST>(s, io, tune, num_sms, st);
 }
 
 void launch_trace_any(const SceneView& s, const float4* rays, int64_t n, uint8_t* occ, TraceCounters* ctr,
-                      int num_sms, cudaStream_t st) {
+                      unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     if (n <= 0) return;
-    count_launches(1);
-    if (ctr) trace_any_kernel<true><<<grid_for(n, num_sms), 256, 0, st>>>(s, rays, n, occ, ctr);
-    else trace_any_kernel<false><<<grid_for(n, num_sms), 256, 0, st>>>(s, rays, n, occ, ctr);
+    TraceIO io{};
+    io.rays = rays;
+    io.occ = occ;
+    io.n = n;
+    io.counter = counter;
+    io.ctr = ctr;
+    launch_mode<MODE_ANY>(s, io, tune, num_sms, st);
 }
 
 void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
-                         float4* shadow_rays, TraceCounters* ctr, int num_sms, cudaStream_t st) {
+                         float4* shadow_rays, TraceCounters* ctr, unsigned long long* counter,
+                         const TraceTuning& tune, int num_sms, cudaStream_t st, int diffuse,
+                         unsigned long long seed) {
     const int64_t n = (int64_t)cam.width * cam.height;
     if (n <= 0) return;
+    TraceIO io{};
+    io.diffuse = diffuse;
+    io.seed = seed;
+    io.hits = hits;
+    io.shadow_rays = shadow_rays;
+    io.cam = cam;
+    io.light = light ? make_float3(light[0], light[1], light[2]) : make_float3(0.f, 0.f, 0.f);
+    io.has_light = light != nullptr;
+    io.n = n;
+    io.counter = counter;
+    io.ctr = ctr;
+    launch_mode<MODE_CAMERA>(s, io, tune, num_sms, st);
+}
+
+template <int ER>
+static void launch_batch_er(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
+                            unsigned long long* counter, int num_sms, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_batch_kernel<ER>, 128, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    long long blocks = (total + 127) / 128;
+    blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
+    if (blocks < 1) blocks = 1;
+    trace_batch_kernel<ER><<<(int)blocks, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, total, counter);
+}
+
+void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
+                        unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+    if (total <= 0 || ntasks <= 0) return;
     count_launches(1);
-    const float3 L = light ? make_float3(light[0], light[1], light[2]) : make_float3(0.f, 0.f, 0.f);
-    if (ctr)
-        trace_camera_kernel<true><<<grid_for(n, num_sms), 256, 0, st>>>(s, cam, hits, L, light != nullptr,
-                                                                         shadow_rays, ctr);
-    else
-        trace_camera_kernel<false><<<grid_for(n, num_sms), 256, 0, st>>>(s, cam, hits, L, light != nullptr,
-                                                                          shadow_rays, ctr);
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
+    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
+    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
 }
 
 void launch_deform(const float* base, const float* normals, float* out, int64_t nverts, float amp, float freq,

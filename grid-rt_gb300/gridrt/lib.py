@@ -22,6 +22,8 @@ RTG_NOT_BUILT = 6
 RTG_INVALID_GEOMETRY = 7
 
 RTG_TRACE_COUNTERS = 1
+RTG_TUNE_EMPTY_RUN = 1
+RTG_TUNE_PERSISTENT = 2
 ORDER = {"scanline": 0, "morton8": 1}
 
 
@@ -40,6 +42,25 @@ class GridInfo(C.Structure):
         return dict(res=tuple(self.res), bmin=np.array(self.bmin, np.float32), bmax=np.array(self.bmax, np.float32),
                     cell=np.array(self.cell, np.float32), inv_cell=np.array(self.inv_cell, np.float32),
                     ncells=int(self.ncells), nrefs=int(self.nrefs), k=int(self.k), built=bool(self.built))
+
+
+class TraceTaskC(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("mode", C.c_int32), ("d_rays", C.c_void_p), ("n", C.c_int64),
+                ("d_out", C.c_void_p)]
+
+
+class RequestC(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("scene", C.c_int32), ("mode", C.c_int32), ("h_rays", C.c_void_p),
+                ("n", C.c_int64), ("h_out", C.c_void_p)]
+
+
+class RequestTimesC(C.Structure):
+    _fields_ = [("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServeOptionsC(C.Structure):
+    _fields_ = [("pool_bytes", C.c_int64), ("max_step_rays", C.c_int64), ("max_in_flight", C.c_int32),
+                ("plain", C.c_int32), ("empty_run", C.c_int32), ("pad", C.c_int32)]
 
 
 class CameraC(C.Structure):
@@ -66,9 +87,11 @@ EXPORTS = [
     "rtg_scene_deform_vertices", "rtg_scene_build", "rtg_scene_build_async", "rtg_scene_build_check",
     "rtg_scene_reserve", "rtg_scene_grid_info", "rtg_scene_grid_download", "rtg_scene_download_vertices", "rtg_scene_grid_device",
     "rtg_trace_nearest", "rtg_trace_nearest_device", "rtg_trace_any", "rtg_trace_any_device",
-    "rtg_trace_camera_device", "rtg_trace_frame_device", "rtg_trace_frame", "rtg_grid_build_noalloc",
+    "rtg_trace_camera_device", "rtg_trace_camera_diffuse_device", "rtg_trace_frame_device", "rtg_trace_frame", "rtg_grid_build_noalloc",
     "rtg_kernel_launch_count",
-    "rtg_scene_counters",
+    "rtg_scene_set_tuning", "rtg_scene_counters", "rtg_batch_create", "rtg_batch_build_async",
+    "rtg_batch_trace_async", "rtg_batch_check", "rtg_batch_rays", "rtg_batch_set_tuning", "rtg_batch_destroy",
+    "rtg_serve_run",
 ]
 
 
@@ -111,11 +134,23 @@ def load(build_if_missing: bool = True):
         "rtg_trace_any": ([vp, vp, i64, vp, i32, vp], C.c_int),
         "rtg_trace_any_device": ([vp, vp, i64, vp, i32, vp], C.c_int),
         "rtg_trace_camera_device": ([vp, C.POINTER(CameraC), vp, vp, vp, i32, vp], C.c_int),
+        "rtg_trace_camera_diffuse_device": ([vp, C.POINTER(CameraC), C.c_uint64, vp, vp, i32, vp], C.c_int),
         "rtg_trace_frame_device": ([vp, C.POINTER(CameraC), vp, vp, vp, vp, vp], C.c_int),
         "rtg_trace_frame": ([vp, C.POINTER(CameraC), vp, vp, vp, vp], C.c_int),
         "rtg_grid_build_noalloc": ([vp, i64, vp, i64, i32, vp, i64, vp, i64, vp, C.POINTER(GridInfo), vp],
                                    C.c_int),
         "rtg_kernel_launch_count": ([], C.c_uint64),
+        "rtg_scene_set_tuning": ([vp, i32, i32], C.c_int),
+        "rtg_batch_create": ([C.POINTER(vp), i32, C.POINTER(i32), C.POINTER(TraceTaskC), i32, C.POINTER(vp)],
+                             C.c_int),
+        "rtg_batch_build_async": ([vp, vp], C.c_int),
+        "rtg_batch_trace_async": ([vp, vp], C.c_int),
+        "rtg_batch_check": ([vp, vp], C.c_int),
+        "rtg_batch_rays": ([vp, C.POINTER(i64)], C.c_int),
+        "rtg_batch_set_tuning": ([vp, i32, i32], C.c_int),
+        "rtg_batch_destroy": ([vp], C.c_int),
+        "rtg_serve_run": ([C.POINTER(vp), i32, C.POINTER(RequestC), i64, C.POINTER(ServeOptionsC),
+                           C.POINTER(RequestTimesC)], C.c_int),
         "rtg_scene_counters": ([vp, C.POINTER(C.c_int64), C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -254,6 +289,12 @@ class Scene:
         check(load().rtg_trace_camera_device(self.h, C.byref(cs), _ptr(d_hits), lp, _ptr(d_shadow_rays),
                                              RTG_TRACE_COUNTERS if counters else 0, stream))
 
+    def trace_camera_diffuse_device(self, cam, seed: int, d_hits, d_secondary, order: str = "scanline",
+                                    counters: bool = False, stream=None):
+        cs = camera_struct(cam, order)
+        check(load().rtg_trace_camera_diffuse_device(self.h, C.byref(cs), int(seed), _ptr(d_hits), _ptr(d_secondary),
+                                                     RTG_TRACE_COUNTERS if counters else 0, stream))
+
     def trace_frame_device(self, cam, light, d_hits, d_occ, d_shadow_rays, order: str = "scanline", stream=None):
         cs = camera_struct(cam, order)
         self._light = np.ascontiguousarray(light, np.float32)
@@ -267,10 +308,88 @@ class Scene:
         check(load().rtg_trace_frame(self.h, C.byref(cs), _ptr(self._light), _ptr(hits_host), _ptr(occ_host),
                                      stream))
 
+    def set_tuning(self, empty_run: int = None, persistent: bool = None):
+        if empty_run is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
+        if persistent is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_PERSISTENT, 1 if persistent else 0))
+
     def counters(self, reset: bool = True):
         out = (C.c_int64 * 3)()
         check(load().rtg_scene_counters(self.h, out, 1 if reset else 0))
         return dict(rays=out[0], cells=out[1], tests=out[2])
+
+
+RTG_MODE_NEAREST = 0
+RTG_MODE_ANY = 1
+
+
+class Batch:
+    """Scenes built together and traced together (rtg_batch_*).  `tasks` is a
+    list of (scene_index, mode, d_rays, n, d_out) with device buffers (torch
+    tensors or raw pointers)."""
+
+    def __init__(self, scenes, ks, tasks):
+        L = load()
+        self._scenes = list(scenes)      # keep the scene objects alive
+        self._keep = [t for t in tasks]
+        arr = (C.c_void_p * len(scenes))(*[sc.h.value for sc in scenes])
+        karr = (C.c_int32 * len(scenes))(*[int(k) for k in ks])
+        tarr = (TraceTaskC * max(len(tasks), 1))()
+        for i, (si, mode, rays, n, out) in enumerate(tasks):
+            tarr[i] = TraceTaskC(int(si), int(mode), _ptr(rays), int(n), _ptr(out))
+        h = C.c_void_p()
+        check(L.rtg_batch_create(arr, len(scenes), karr, tarr, len(tasks), C.byref(h)))
+        self.h = h
+
+    def build_async(self, stream=None):
+        check(load().rtg_batch_build_async(self.h, stream))
+
+    def trace_async(self, stream=None):
+        check(load().rtg_batch_trace_async(self.h, stream))
+
+    def check(self, stream=None) -> int:
+        return load().rtg_batch_check(self.h, stream)
+
+    def rays(self) -> int:
+        r = C.c_int64()
+        check(load().rtg_batch_rays(self.h, C.byref(r)))
+        return r.value
+
+    def set_tuning(self, empty_run: int = None, persistent: bool = None):
+        if empty_run is not None:
+            check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
+        if persistent is not None:
+            check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_PERSISTENT, 1 if persistent else 0))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().rtg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def serve(scenes, requests, pool_bytes: int, plain: bool = False, max_in_flight: int = 3,
+          max_step_rays: int = 0, empty_run: int = 0):
+    """Runs rtg_serve_run.  requests: list of (arrival_s, scene_index, mode,
+    h_rays, n, h_out) with pinned host buffers (torch pinned tensors or
+    pointers).  Returns (admit_s, done_s) arrays."""
+    L = load()
+    arr = (C.c_void_p * len(scenes))(*[sc.h.value for sc in scenes])
+    reqs = (RequestC * max(len(requests), 1))()
+    for i, (t, si, mode, rays, n, out) in enumerate(requests):
+        reqs[i] = RequestC(float(t), int(si), int(mode), _ptr(rays), int(n), _ptr(out))
+    times = (RequestTimesC * max(len(requests), 1))()
+    opt = ServeOptionsC(int(pool_bytes), int(max_step_rays), int(max_in_flight), 1 if plain else 0, int(empty_run), 0)
+    check(L.rtg_serve_run(arr, len(scenes), reqs, len(requests), C.byref(opt), times))
+    admit = np.array([times[i].admit_s for i in range(len(requests))])
+    done = np.array([times[i].done_s for i in range(len(requests))])
+    return admit, done
 
 
 def kernel_launches() -> int:

@@ -268,3 +268,38 @@ def tiny_scene(seed: int, ntris: int, spread: float = 1.0, size: float = 0.2) ->
     tri = random_triangles(rng, ntris, (-spread,) * 3, (spread,) * 3, size)
     return Scene(verts=np.ascontiguousarray(tri.reshape(-1, 3)),
                  idx=np.arange(3 * ntris, dtype=np.int32).reshape(ntris, 3), name=f"tiny[{seed}]")
+
+
+@dataclasses.dataclass
+class BatchItem:
+    scene: Scene
+    rays: np.ndarray        # (R, 8) float32: primary pinhole rays first, then random rays
+    n_primary: int
+    camera: Camera
+
+
+def batched_workload(seed: int = SEED_BASE + 3, nscenes: int = 64, tri_range=(1_000, 500_000),
+                     ray_range=(4_000, 1_000_000), primary_frac: float = 0.6, order: str = "scanline"):
+    """Uneven batch: scenes built like plane_and_debris with triangle counts
+    log-uniform in tri_range (half ground-plane quads, half debris), each with
+    a ray batch log-uniform in ray_range: primary_frac pinhole rays (square
+    image, pixel centres, eye/target of the plane scene) and the rest random
+    directions from uniform origins in the scene box."""
+    rng = _rng(seed)
+    items = []
+    for i in range(nscenes):
+        n_tri = int(round(math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))))
+        quads = max(2, int(round(math.sqrt(n_tri / 4.0))))
+        debris = max(1, n_tri - 2 * quads * quads)
+        sc = plane_and_debris(seed=seed * 1000 + i, quads=quads, debris=debris)
+        n_ray = int(round(math.exp(rng.uniform(math.log(ray_range[0]), math.log(ray_range[1])))))
+        side = max(8, int(round(math.sqrt(primary_frac * n_ray) / 8.0)) * 8)
+        cam = plane_and_debris_camera(side, side)
+        prim = camera_rays(cam, order)
+        n_rand = max(0, n_ray - prim.shape[0])
+        lo = sc.verts.min(axis=0)
+        hi = sc.verts.max(axis=0)
+        rnd = random_rays(rng, n_rand, lo, hi)
+        items.append(BatchItem(scene=sc, rays=np.ascontiguousarray(np.concatenate([prim, rnd], axis=0)),
+                               n_primary=prim.shape[0], camera=cam))
+    return items

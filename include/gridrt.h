@@ -181,6 +181,14 @@ rtg_status rtg_trace_any_device(rtg_scene scene, const float* d_rays, int64_t n,
  * get tmax = -1.  n is the flat normal turned to face the incoming ray. */
 rtg_status rtg_trace_camera_device(rtg_scene scene, const rtg_camera* cam, rtg_hit* d_hits,
                                    const float* light_pos, float* d_shadow_rays, int32_t flags, void* stream);
+/* Camera closest hits plus one cosine-weighted diffuse secondary ray per hit
+ * (origin P + n*2e-4 with the flat normal n turned toward the incoming ray,
+ * tnear 2e-4, tfar FLT_MAX; random bits from a counter-based hash of `seed`
+ * and the ray index).  Pixels without a hit get a ray with tfar = -1, which
+ * the trace calls report as a miss.  No counterpart in the reference's CPU
+ * path; it feeds the skewed-density workload's secondary rays. */
+rtg_status rtg_trace_camera_diffuse_device(rtg_scene scene, const rtg_camera* cam, uint64_t seed, rtg_hit* d_hits,
+                                           float* d_secondary_rays, int32_t flags, void* stream);
 /* Primary + shadow frame: camera closest hits, shadow rays and any-hit in one
  * call on the device.  occluded[i]: 0 lit, 1 shadowed, 2 no shadow ray. */
 rtg_status rtg_trace_frame_device(rtg_scene scene, const rtg_camera* cam, const float* light_pos,
@@ -217,6 +225,82 @@ rtg_status rtg_grid_build_noalloc(const float* d_verts, int64_t nverts, const in
 
 /* Number of CUDA kernels this library has launched in this process. */
 uint64_t rtg_kernel_launch_count(void);
+
+/* ---- batches: many scenes built and traced together ----------------------
+ * A batch plan fixes a set of scenes (up to 64, same device, each non-empty)
+ * and a set of trace tasks; its device tables are uploaded once, so the two
+ * enqueue calls below can run every frame or be captured in a CUDA graph.
+ *   rtg_batch_build_async: every scene's grid in one set of build kernels
+ *     (block row y builds scene y); same result as rtg_scene_build per scene.
+ *   rtg_batch_trace_async: every task in one persistent trace launch; warps
+ *     claim 32-ray slices of the concatenated tasks.
+ *   rtg_batch_check: synchronises and reports whether every build since the
+ *     last check fitted its scene's buffers (RTG_NO_MEMORY otherwise: rebuild
+ *     the scenes with rtg_scene_build and recreate the plan).
+ * The enqueue calls re-upload a scene's table entry (synchronously) when its
+ * buffers moved since the last call, e.g. after a growing rtg_scene_build; a
+ * CUDA graph captured from them keeps the addresses it saw, so do not let the
+ * scenes' buffers grow while such a graph is in use (rtg_scene_reserve). */
+typedef struct rtg_batch_s* rtg_batch;
+enum { RTG_MODE_NEAREST = 0, RTG_MODE_ANY = 1 };
+typedef struct {
+    int32_t scene;        /* index into the scenes array of rtg_batch_create */
+    int32_t mode;         /* RTG_MODE_NEAREST (rtg_hit out) or RTG_MODE_ANY (uint8 out) */
+    const float* d_rays;  /* n x 8 float32, device */
+    int64_t n;
+    void* d_out;          /* device output: n rtg_hit or n uint8 */
+} rtg_trace_task;
+/* k[i]: cells per triangle for scene i.  Scenes are built once here
+ * (synchronously) to size their buffers. */
+rtg_status rtg_batch_create(const rtg_scene* scenes, int32_t nscenes, const int32_t* k, const rtg_trace_task* tasks,
+                            int32_t ntasks, rtg_batch* out);
+rtg_status rtg_batch_build_async(rtg_batch batch, void* stream);
+rtg_status rtg_batch_trace_async(rtg_batch batch, void* stream);
+rtg_status rtg_batch_check(rtg_batch batch, void* stream);
+/* Total rays over the batch's tasks. */
+rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
+rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
+rtg_status rtg_batch_destroy(rtg_batch batch);
+
+/* ---- serving: continuous batching over resident scenes ------------------
+ * rtg_serve_run replays a stream of ray-query requests in real time against
+ * built, resident scenes (up to 64, one device) and reports, per request, when
+ * it was admitted and when its results were back in host memory.  Requests
+ * are admitted in arrival order while a device pool of opt->pool_bytes has
+ * room for their rays (32 B/ray) and results (16 B or 1 B per ray); the
+ * admitted requests form one step: uploads, ONE persistent trace launch over
+ * all of them, downloads, on the step's own stream, up to opt->max_in_flight
+ * steps on the GPU at once.  opt->plain = 1 instead serves one request at a
+ * time through the single-scene trace (the per-request baseline).
+ * h_rays / h_out must be pinned host memory; arrivals must be sorted. */
+typedef struct {
+    double arrival_s;     /* seconds after the start of the run */
+    int32_t scene;        /* index into the scenes array */
+    int32_t mode;         /* RTG_MODE_NEAREST or RTG_MODE_ANY (occlusion before each ray's tfar) */
+    const float* h_rays;  /* n x 8 float32, pinned host */
+    int64_t n;
+    void* h_out;          /* n rtg_hit or n uint8 (0 lit, 1 occluded, 2 no ray), pinned host */
+} rtg_request;
+typedef struct {
+    double admit_s;       /* its step was launched */
+    double done_s;        /* its results were back in host memory */
+} rtg_request_times;
+typedef struct {
+    int64_t pool_bytes;       /* device memory for requests in flight */
+    int64_t max_step_rays;    /* rays per step at most (0: 16M) */
+    int32_t max_in_flight;    /* steps on the GPU at once, 1..8 */
+    int32_t plain;            /* 1: one request at a time, single-scene trace */
+    int32_t empty_run;        /* trace tuning, 0 = the first scene's */
+    int32_t pad;
+} rtg_serve_options;
+rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_request* reqs, int64_t nreq,
+                         const rtg_serve_options* opt, rtg_request_times* times);
+
+/* Trace launch shape for this scene (results never depend on it):
+ *   RTG_TUNE_EMPTY_RUN   empty cells a ray may walk per loop turn: 4, 8, 16 (default 8)
+ *   RTG_TUNE_PERSISTENT  1: persistent warps claim ray batches (default); 0: one batch per warp */
+enum { RTG_TUNE_EMPTY_RUN = 1, RTG_TUNE_PERSISTENT = 2 };
+rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 
 /* Counters accumulated by calls made with RTG_TRACE_COUNTERS since the last
  * reset: out[0] = rays, out[1] = cells visited, out[2] = triangle tests. */
