@@ -292,11 +292,10 @@ def run_gpu(args, rank, ws, local, dist):
             s.build_async(k)
             if ev:
                 ev[1].record(stream)
-            s.trace_camera_device(cam, d_hits, light=light, d_shadow_rays=d_sr, order=order)
+            # primary rays, then each hit's shadow ray (any-hit)
+            s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order)
             if ev:
                 ev[2].record(stream)
-            s.trace_any_device(d_sr, npix, d_occ)
-            if ev:
                 ev[3].record(stream)
 
     # autotune the trace launch shape and ray order per k (results do not
@@ -305,7 +304,7 @@ def run_gpu(args, rank, ws, local, dist):
 
     def tune_k(k):
         def measure(cfg):
-            s.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"])
+            _apply_tuning(s, cfg)
             evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             frame(k, 0, cfg["order"])
             frame(k, 1, cfg["order"], evs)
@@ -314,13 +313,17 @@ def run_gpu(args, rank, ws, local, dist):
         return autotune.search(measure, reps=3)
 
     tuned = {}
+    fixed = _parse_tuning(args.fixed_tuning)
     per_k = {}
     sampler = ClockSampler(local).start() if rank == 0 else None
-    for k in LAMBDAS:
-        best, allres = tune_k(k)
+    for k in ([fixed["k"]] if fixed else LAMBDAS):
+        if fixed:
+            best, allres = {x: fixed[x] for x in fixed if x != "k"}, []
+        else:
+            best, allres = tune_k(k)
         tuned[k] = dict(best=best, all=[(c, round(m, 4)) for c, m in allres])
         order = best["order"]
-        s.set_tuning(empty_run=best["empty_run"], persistent=best["persistent"])
+        _apply_tuning(s, best)
         for w in range(args.warmup):
             frame(k, w % FRAMES, order)
         torch.cuda.synchronize()
@@ -338,7 +341,7 @@ def run_gpu(args, rank, ws, local, dist):
                 flush.zero_()                      # L2 flush between frames (outside the events)
             frame(k, st % FRAMES, order, evs[st])
             with torch.cuda.stream(stream):
-                shadow_count += (d_sr[:, 7] >= 0).sum()
+                shadow_count += (d_occ != 2).sum()
         lc1 = lib.kernel_launches()
         torch.cuda.synchronize()
         _barrier(dist)
@@ -347,15 +350,15 @@ def run_gpu(args, rank, ws, local, dist):
         if s.build_check() != 0:
             raise RuntimeError("timed build failed: " + lib.load().rtg_last_error().decode())
         build_ms = [e[0].elapsed_time(e[1]) for e in evs]
-        prim_ms = [e[1].elapsed_time(e[2]) for e in evs]
-        shad_ms = [e[2].elapsed_time(e[3]) for e in evs]
+        prim_ms = [e[1].elapsed_time(e[2]) for e in evs]   # primary + shadow launches
+        shad_ms = [0.0 for e in evs]
         frame_ms = [e[0].elapsed_time(e[3]) for e in evs]
         total_s = _max_over_ranks(sum(frame_ms) / 1e3, dist)
         rays = npix * args.steps + int(shadow_count.item())
         rays_all = _sum_over_ranks(rays, dist)
         per_k[k] = dict(tuning=best, value=rays_all / total_s / 1e6, ms_per_step=1e3 * total_s / args.steps,
-                        build_ms=statistics.median(build_ms), primary_ms=statistics.median(prim_ms),
-                        shadow_ms=statistics.median(shad_ms), rays_per_step=rays / args.steps,
+                        build_ms=statistics.median(build_ms), trace_ms=statistics.median(prim_ms),
+                        rays_per_step=rays / args.steps,
                         trace_mrays_s=rays / (sum(prim_ms) + sum(shad_ms)) / 1e3,
                         launches=lc1 - lc0)
     if sampler:
@@ -364,30 +367,40 @@ def run_gpu(args, rank, ws, local, dist):
     best_k = max(per_k, key=lambda kk: per_k[kk]["value"])
     head = per_k[best_k]
     order = head["tuning"]["order"]
-    s.set_tuning(empty_run=head["tuning"]["empty_run"], persistent=head["tuning"]["persistent"])
+    _apply_tuning(s, head["tuning"])
 
     # roofline of the dominant kernel (primary camera trace): algorithmic bytes
     # from the traversal counters (16 B hit + 8 B per visited cell + 52 B per
     # triangle test: 4 B list entry + 48 B record), camera rays read 0 B
     s.deform(d_base, d_nrm, 0.05, 3.0, 0.0)
     s.build(best_k)
+    # counters of the frame's two ray generations: primary rays (camera
+    # kernel) and their shadow rays (any-hit over the same shadow rays)
     s.counters(reset=True)
     s.trace_camera_device(cam, d_hits, light=light, d_shadow_rays=d_sr, order=order, counters=True)
-    c = s.counters(reset=True)
-    alg_bytes = 16 * c["rays"] + 8 * c["cells"] + 52 * c["tests"]
-    # the kernel's own average duration (events around the launch alone)
+    c1 = s.counters(reset=True)
+    s.trace_any_device(d_sr, npix, d_occ, counters=True)
+    c2 = s.counters(reset=True)
+    n_shadow = int((d_sr[:, 7] >= 0).sum().item())
+    c = {"rays": c1["rays"] + n_shadow, "cells": c1["cells"] + c2["cells"], "tests": c1["tests"] + c2["tests"]}
+    # per pixel: 16 B hit and 32 B shadow-ray slot written by the camera
+    # launch, the 32 B slot read and 1 B occlusion written by the any-hit
+    # launch; 8 B per visited cell (occupancy word + list bounds), 52 B per
+    # triangle test (4 B id + 48 B record); camera rays are generated, 0 B
+    alg_bytes = (16 + 32 + 32 + 1) * npix + 8 * c["cells"] + 52 * c["tests"]
+    # the frame's two trace launches, averaged (events around the launches alone)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 10
     with torch.cuda.stream(stream):
         ev0.record(stream)
         for _ in range(reps):
-            s.trace_camera_device(cam, d_hits, light=light, d_shadow_rays=d_sr, order=order)
+            s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order)
         ev1.record(stream)
     torch.cuda.synchronize()
     kern_s = ev0.elapsed_time(ev1) / 1e3 / reps
     peak, peak_kind = _peaks()
     achieved = alg_bytes / kern_s / 1e9
-    traffic = _traffic_from_profiles("trace_camera_kernel", alg_bytes)
+    traffic = _traffic_from_profiles("trace_frame", alg_bytes)
 
     # e2e through the public C ABI with host buffers
     e2e = run_e2e(args, s, v, idx, nrm, cam, light, best_k, order, dist)
@@ -413,7 +426,9 @@ def run_gpu(args, rank, ws, local, dist):
         "autotune": {str(kk): v["all"] for kk, v in tuned.items()},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "trace_camera_kernel", "alg_bytes_per_launch": int(alg_bytes),
+                     "kernel": "trace_kernel camera + any, with their warp-per-ray passes when enabled "
+                               "(one frame's trace launches)",
+                     "alg_bytes_per_launch": int(alg_bytes),
                      "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"])},
         "cpu_baseline": {"value": round(cpu["rays"] / cpu["t_frame"] / 1e6, 4), "unit": "Mrays/s",
                          "cores": cpu["threads"], "kind": "port",
@@ -549,6 +564,38 @@ def run_batched(args, rank, ws, local, dist):
             sc.trace_nearest_device(d_rays[best["order"]][i], base[i].rays.shape[0], d_hits[i])
         torch.cuda.synchronize()
 
+    # breakdown: batched build alone, batched trace alone, plain builds alone,
+    # plain traces alone (each timed separately, outside the headline numbers)
+    def graph_ms(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        g2 = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g2, stream=stream):
+            fn()
+        g2.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(reps):
+                g2.replay()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    breakdown = {"batched_build_ms": graph_ms(lambda: b.build_async(stream.cuda_stream)),
+                 "batched_trace_ms": graph_ms(lambda: b.trace_async(stream.cuda_stream))}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for sc in scs:
+        sc.build(best["k"])
+    breakdown["plain_build_ms"] = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    for i, sc in enumerate(scs):
+        sc.trace_nearest_device(d_rays[best["order"]][i], base[i].rays.shape[0], d_hits[i])
+    torch.cuda.synchronize()
+    breakdown["plain_trace_ms"] = (time.perf_counter() - t0) * 1e3
+
     for _ in range(args.warmup):
         plain_pass()
     reps = max(3, args.steps // 10)
@@ -569,8 +616,115 @@ def run_batched(args, rank, ws, local, dist):
         "plain": {"value": round(rays_all / plain_ms / 1e3, 3), "unit": "Mrays/s", "ms_per_step": round(plain_ms, 4),
                   "how": "per scene: rtg_scene_build (synchronous) + rtg_trace_nearest_device, 64 in sequence"},
         "batched_over_plain": round(plain_ms / batched_ms, 3),
+        "breakdown_ms": {k_: round(v_, 4) for k_, v_ in breakdown.items()},
         "autotune": [(c, round(m, 4)) for c, m in allres],
     }), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# serving: 16 resident scenes, Poisson request streams, continuous batching
+# (rtg_serve_run) versus the plain one-request-at-a-time path
+# ---------------------------------------------------------------------------
+def run_serving(args, rank, ws, local, dist):
+    import torch
+    from gridrt import lib
+
+    torch.cuda.set_device(local)
+    rng = np.random.Generator(np.random.PCG64(scenes.SEED_BASE + 4))
+    nscenes = 16
+    scs, scene_bytes, tris = [], 0, 0
+    for i in range(nscenes):
+        n_tri = int(round(np.exp(rng.uniform(np.log(10_000), np.log(1_000_000)))))
+        quads = max(2, int(round(np.sqrt(n_tri / 4.0))))
+        sc = scenes.plane_and_debris(seed=scenes.SEED_BASE + 400 + i, quads=quads, debris=max(1, n_tri - 2 * quads * quads))
+        s = lib.Scene(local)
+        s.set_geometry(sc.verts, sc.idx)
+        s.build(4)
+        inf = s.info()
+        scene_bytes += 12 * sc.nverts + 12 * sc.ntris + 48 * sc.ntris + 8 * (inf["ncells"] + 1) + 8 * inf["nrefs"]
+        tris += sc.ntris
+        scs.append(s)
+    # ray pools shared by all requests (every scene spans [-1,1] x [0,1] x [-1,1])
+    pool_n = 4_000_000
+    cam = scenes.plane_and_debris_camera(2000, 1000)
+    near = np.concatenate([scenes.camera_rays(cam), scenes.random_rays(rng, pool_n - 2_000_000, (-1, 0, -1), (1, 1, 1))])
+    anyr = scenes.random_rays(rng, pool_n, (-1, 0, -1), (1, 1, 1))
+    anyr[:, 7] = 1.0
+    h_near = torch.from_numpy(near).pin_memory()
+    h_any = torch.from_numpy(anyr).pin_memory()
+    h_out = torch.empty(16 * pool_n, dtype=torch.uint8).pin_memory()
+    budget = 40 << 30
+    pool_bytes = int(min(8 << 30, budget - scene_bytes))
+
+    def make_requests(rate, count, seed):
+        r = np.random.Generator(np.random.PCG64(seed))
+        t = 0.0 if rate is None else np.cumsum(r.exponential(1.0 / rate, size=count))
+        reqs = []
+        for i in range(count):
+            n = int(round(np.exp(r.uniform(np.log(1_000), np.log(4_000_000)))))
+            off = int(r.integers(0, pool_n - n + 1))
+            si = int(r.integers(0, nscenes))
+            if r.uniform() < 0.3:
+                mode, src = lib.RTG_MODE_ANY, h_any
+            else:
+                mode, src = lib.RTG_MODE_NEAREST, h_near
+            arr = 0.0 if rate is None else float(t[i])
+            reqs.append((arr, si, mode, src.data_ptr() + 32 * off, n, h_out))
+        return reqs
+
+    def run(reqs, plain):
+        admit, done = lib.serve(scs, reqs, pool_bytes=pool_bytes, plain=plain, max_in_flight=3)
+        arr = np.array([q[0] for q in reqs])
+        lat = done - arr
+        rays = sum(q[4] for q in reqs)
+        span = done.max() - arr.min()
+        return dict(p50_ms=round(1e3 * float(np.percentile(lat, 50)), 3),
+                    p99_ms=round(1e3 * float(np.percentile(lat, 99)), 3),
+                    mrays_s=round(rays / span / 1e6, 2), requests=len(reqs), rays=int(rays))
+
+    # warm up both paths
+    wu = make_requests(None, 20, 1)
+    run(wu, False)
+    run(wu, True)
+    rates = [10, 100, 1000, 2000]
+    out = {}
+    for rate in rates:
+        count = int(min(10_000, rate * args.serve_seconds))
+        reqs = make_requests(rate, count, 100 + rate)
+        out[str(rate)] = {"served": run(reqs, False), "plain": run(reqs, True)}
+    sat = make_requests(None, args.serve_saturation, 7)
+    saturation = {"served": run(sat, False), "plain": run(sat, True)}
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "Mrays/s at saturation (served) + p50/p99 latency", "value": saturation["served"]["mrays_s"],
+        "unit": "Mrays/s", "n_gpus": ws, "steps": len(rates), "warmup": 1, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "serving_16_scenes", "scenes": nscenes, "triangles": tris,
+                   "scene_bytes": int(scene_bytes), "pool_bytes": pool_bytes, "hbm_budget_bytes": budget,
+                   "rays_per_request": "log-uniform [1e3, 4e6]", "modes": "70% closest / 30% any-hit",
+                   "max_in_flight": 3},
+        "saturation": saturation, "served_over_plain": round(saturation["served"]["mrays_s"] /
+                                                              saturation["plain"]["mrays_s"], 3),
+        "rates": out,
+    }), flush=True)
+
+
+def _parse_tuning(text):
+    """'k=8,order=morton8,empty_run=4,persistent=0,heavy_cell=32,cell_records=1' -> dict, or None."""
+    if not text:
+        return None
+    d = dict(kv.split("=", 1) for kv in text.split(","))
+    yes = lambda v: v not in ("0", "false", "False")
+    return {"k": int(d.get("k", 8)), "order": d.get("order", "morton8"), "empty_run": int(d.get("empty_run", 4)),
+            "persistent": yes(d.get("persistent", "0")), "heavy_cell": int(d.get("heavy_cell", 0)),
+            "cell_records": yes(d.get("cell_records", "0"))}
+
+
+def _apply_tuning(scene, cfg):
+    """Launch-shape settings of one candidate; cell records take effect at the next build."""
+    scene.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"],
+                     heavy_cell=cfg.get("heavy_cell", 0), cell_records=cfg.get("cell_records", False))
 
 
 def main():
@@ -579,7 +733,11 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
-    ap.add_argument("--workload", default="deforming", choices=["deforming", "batched"])
+    ap.add_argument("--workload", default="deforming", choices=["deforming", "batched", "serving"])
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
+    ap.add_argument("--serve-saturation", type=int, default=2000)
+    ap.add_argument("--fixed-tuning", default="",
+                    help="skip the autotuner: e.g. k=8,order=morton8,empty_run=4,persistent=0 (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, ws, local, dist = _dist()
@@ -587,6 +745,8 @@ def main():
         run_reference(args, rank, ws, dist)
     elif args.workload == "batched":
         run_batched(args, rank, ws, local, dist)
+    elif args.workload == "serving":
+        run_serving(args, rank, ws, local, dist)
     else:
         run_gpu(args, rank, ws, local, dist)
     if dist is not None:

@@ -59,7 +59,12 @@ rtg_status set_device(rtg_scene s) {
     return RTG_OK;
 }
 
-int64_t ref_capacity(const rtg_scene s) { return s->ids_cap < s->scratch_cap ? s->ids_cap : s->scratch_cap; }
+int64_t ref_capacity(const rtg_scene s) {
+    int64_t c = s->ids_cap < s->scratch_cap ? s->ids_cap : s->scratch_cap;
+    if (s->tune.cell_records) c = c < s->crec_cap / 3 ? c : s->crec_cap / 3;
+    return c;
+}
+
 
 rtg_status ensure_grid_buffers(rtg_scene s, int64_t cells_plus_one, int64_t refs) {
     CUDA_TRY(grow(s->d_offsets, s->cell_cap, cells_plus_one));
@@ -67,11 +72,20 @@ rtg_status ensure_grid_buffers(rtg_scene s, int64_t cells_plus_one, int64_t refs
     CUDA_TRY(grow(s->d_tiles, s->tiles_cap, s->cell_cap / 4096 + 2));
     CUDA_TRY(grow(s->d_ids, s->ids_cap, refs));
     CUDA_TRY(grow(s->d_scratch, s->scratch_cap, refs));
+    if (s->tune.cell_records) CUDA_TRY(grow(s->d_crec, s->crec_cap, 3 * s->ids_cap));
     const int64_t R = ref_capacity(s);
     CUDA_TRY(grow(s->d_qs, s->qs_cap, R / 2 + 2));
     CUDA_TRY(grow(s->d_qm, s->qm_cap, R / 33 + 2));
     CUDA_TRY(grow(s->d_ql, s->ql_cap, R / 4097 + 2));
     return RTG_OK;
+}
+
+// Cell-ordered records enabled after the id buffers were sized: give the
+// record buffer the same capacity before the next build.
+rtg_status ensure_cell_records(rtg_scene s) {
+    const int64_t raw = s->ids_cap < s->scratch_cap ? s->ids_cap : s->scratch_cap;
+    if (!s->tune.cell_records || !s->d_offsets || s->crec_cap >= 3 * raw) return RTG_OK;
+    return ensure_grid_buffers(s, s->cell_cap, raw);
 }
 
 BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
@@ -89,6 +103,7 @@ BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
     a.occ = s->d_occ;
     a.cell_cap = s->cell_cap < s->occ_cap ? s->cell_cap : s->occ_cap;
     a.ids = s->d_ids;
+    a.crec = s->tune.cell_records ? s->d_crec : nullptr;
     a.scratch = s->d_scratch;
     a.ref_cap = ref_capacity(s);
     a.tile_sums = s->d_tiles;
@@ -185,16 +200,21 @@ cudaStream_t pick(rtg_scene s, void* stream) { return stream ? (cudaStream_t)str
 }  // namespace
 
 namespace gridrt {
-// Each trace launch takes the next of kRayCounters device words for its ray
-// hand-out, so up to that many launches may be in flight at once.
-unsigned long long* scene_counter(rtg_scene s) {
+// Each trace launch takes the next of kRayCounters counter slots (and the
+// deferred-ray queue beside it), so up to that many launches may be in
+// flight at once.
+TraceSlot scene_counter(rtg_scene s) {
     const unsigned slot = __atomic_fetch_add(&s->ctr_seq, 1u, __ATOMIC_RELAXED) % kRayCounters;
-    return s->d_ray_ctr + slot;
+    TraceSlot t;
+    t.ctr = s->d_ray_ctr + 4 * (size_t)slot;
+    t.defer = s->d_defer ? s->d_defer + (size_t)slot * kDeferCap : nullptr;
+    t.defer_cap = s->d_defer ? kDeferCap : 0;
+    return t;
 }
 }  // namespace gridrt
 
 namespace {
-unsigned long long* next_counter(rtg_scene s) { return scene_counter(s); }
+TraceSlot next_counter(rtg_scene s) { return scene_counter(s); }
 
 }  // namespace
 
@@ -205,6 +225,7 @@ SceneView scene_view(rtg_scene s) {
     v.offsets = s->d_offsets;
     v.ids = s->d_ids;
     v.occ = s->d_occ;
+    v.crec = (s->tune.cell_records && s->crec_built) ? s->d_crec : nullptr;
     v.tris = s->d_tris;
     return v;
 }
@@ -257,7 +278,7 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
     if (rc == RTG_OK && cudaMallocHost(&s->h_params, sizeof(GridParams)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "pinned");
     if (rc == RTG_OK && cudaMalloc(&s->d_work, sizeof(BuildWork)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "work");
     if (rc == RTG_OK && cudaMalloc(&s->d_ctr, sizeof(TraceCounters)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "ctr");
-    if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
+    if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, 4 * kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
         rc = fail(RTG_NO_MEMORY, "ray counters");
     if (rc == RTG_OK) {
         BuildWork w;
@@ -289,8 +310,10 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
     cudaFree(s->d_offsets);
     cudaFree(s->d_occ);
     cudaFree(s->d_ray_ctr);
+    cudaFree(s->d_defer);
     cudaFree(s->d_ids);
     cudaFree(s->d_scratch);
+    cudaFree(s->d_crec);
     cudaFree(s->d_tiles);
     cudaFree(s->d_qs);
     cudaFree(s->d_qm);
@@ -385,12 +408,15 @@ rtg_status rtg_scene_build_async(rtg_scene s, int32_t k, void* stream) {
     if (s->ntris == 0 || s->nverts == 0) return empty_grid(s, k);
     // The first build of a scene runs synchronously: it sizes the buffers.
     if (!s->d_offsets || s->hp.ncells == 0) return rtg_scene_build(s, k, stream);
+    rc = ensure_cell_records(s);
+    if (rc) return rc;
     rc = enqueue_build(s, k, false, pick(s, stream));
     if (rc) return rc;
     // Trace calls may follow on the same stream: the trace kernels read the
     // device-side status and return misses if this build failed, and
     // rtg_scene_build_check reports the failure.
     s->built = true;
+    s->crec_built = s->tune.cell_records != 0;
     return RTG_OK;
 }
 
@@ -431,6 +457,8 @@ rtg_status rtg_scene_build(rtg_scene s, int32_t k, void* stream) {
         rc = ensure_grid_buffers(s, 1, 1);
         if (rc) return rc;
     }
+    rc = ensure_cell_records(s);
+    if (rc) return rc;
     s->built = false;
     bool skip_bbox = false;
     for (int attempt = 0; attempt < 6; ++attempt) {
@@ -469,6 +497,7 @@ rtg_status rtg_scene_build(rtg_scene s, int32_t k, void* stream) {
             return fail(RTG_INVALID_GEOMETRY, "non-finite vertex or triangle outside the grid");
         s->hp = p;
         s->built = true;
+        s->crec_built = s->tune.cell_records != 0;
         uint32_t sticky = 0;
         return read_clear_sticky(s, &sticky);   // earlier attempts of this call are resolved
     }
@@ -673,10 +702,18 @@ rtg_status rtg_trace_camera_diffuse_device(rtg_scene s, const rtg_camera* cam, u
 
 rtg_status rtg_trace_frame_device(rtg_scene s, const rtg_camera* cam, const float* light_pos, rtg_hit* d_hits,
                                   uint8_t* d_occ, float* d_shadow_rays, void* stream) {
-    if (!light_pos || !d_occ || !d_shadow_rays) return fail(RTG_INVALID_PARAM, "NULL arguments");
-    rtg_status rc = rtg_trace_camera_device(s, cam, d_hits, light_pos, d_shadow_rays, 0, stream);
+    if (!light_pos || !d_occ || !d_hits) return fail(RTG_INVALID_PARAM, "NULL arguments");
+    rtg_status rc = check_traceable(s, 0);
     if (rc) return rc;
+    if (!camera_ok(cam)) return fail(RTG_INVALID_PARAM, "bad camera (size, or Morton order needs multiples of 8)");
     const int64_t n = (int64_t)cam->width * cam->height;
+    if (!d_shadow_rays) {   // the shadow rays need a home between the two passes
+        rc = ensure_io(s, 32 * n + 64);
+        if (rc) return rc;
+        d_shadow_rays = reinterpret_cast<float*>(s->d_io);
+    }
+    rc = rtg_trace_camera_device(s, cam, d_hits, light_pos, d_shadow_rays, 0, stream);
+    if (rc) return rc;
     cudaStream_t st = pick(s, stream);
     if (s->hp.ncells == 0) {
         CUDA_TRY(cudaMemsetAsync(d_occ, 2, n, st));
@@ -697,8 +734,8 @@ rtg_status rtg_trace_frame(rtg_scene s, const rtg_camera* cam, const float* ligh
     const int64_t n = (int64_t)cam->width * cam->height;
     rc = ensure_io(s, n * (16 + 32 + 1) + 64);
     if (rc) return rc;
-    rtg_hit* d_hits = reinterpret_cast<rtg_hit*>(s->d_io);
-    float* d_sr = reinterpret_cast<float*>(s->d_io + n * 16);
+    float* d_sr = reinterpret_cast<float*>(s->d_io);
+    rtg_hit* d_hits = reinterpret_cast<rtg_hit*>(s->d_io + n * 32);
     uint8_t* d_occ = s->d_io + n * 48;
     cudaStream_t st = pick(s, stream);
     rc = rtg_trace_frame_device(s, cam, light_pos, d_hits, d_occ, d_sr, st);
@@ -728,7 +765,9 @@ struct rtg_batch_s {
     long long rays = 0;
     unsigned long long* d_counter = nullptr;
     TraceTuning tune;
-    BuildArgs dims{};
+    int* d_first = nullptr;                // kBuildKinds prefix tables of ntasks + 1 ints
+    BatchGrid grid{};
+    int bitmap_words = 0;
 };
 
 namespace {
@@ -761,15 +800,22 @@ rtg_status batch_upload_build(rtg_batch b, cudaStream_t st, bool force) {
         }
     }
     if (!changed) return RTG_OK;
-    BuildArgs dims{};
-    dims = b->h_build[0];
-    for (const BuildArgs& a : b->h_build) {
-        dims.nverts = a.nverts > dims.nverts ? a.nverts : dims.nverts;
-        dims.ntris = a.ntris > dims.ntris ? a.ntris : dims.ntris;
-        dims.cell_cap = a.cell_cap > dims.cell_cap ? a.cell_cap : dims.cell_cap;
+    // flat batch grids: per kernel kind, the tasks' single-scene block counts back to back
+    const int nt = (int)b->h_build.size();
+    std::vector<int> first((size_t)kBuildKinds * (nt + 1));
+    for (int k = 0; k < kBuildKinds; ++k) first[(size_t)k * (nt + 1)] = 0;
+    for (int t = 0; t < nt; ++t) {
+        int blocks[kBuildKinds];
+        build_blocks(b->h_build[t], b->num_sms, blocks);
+        for (int k = 0; k < kBuildKinds; ++k)
+            first[(size_t)k * (nt + 1) + t + 1] = first[(size_t)k * (nt + 1) + t] + blocks[k];
     }
-    dims.skip_bbox = false;
-    b->dims = dims;
+    for (int k = 0; k < kBuildKinds; ++k) {
+        b->grid.total[k] = first[(size_t)k * (nt + 1) + nt];
+        b->grid.first[k] = b->d_first + (size_t)k * (nt + 1);
+    }
+    b->bitmap_words = b->h_build[0].bitmap_words;
+    CUDA_TRY(cudaMemcpyAsync(b->d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(b->d_build, b->h_build.data(), sizeof(BuildArgs) * b->h_build.size(),
                              cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));   // the host copy may change before the next upload
@@ -830,7 +876,8 @@ rtg_status rtg_batch_create(const rtg_scene* scenes, int32_t nscenes, const int3
     if (cudaMalloc(&b->d_build, sizeof(BuildArgs) * nscenes) != cudaSuccess ||
         cudaMalloc(&b->d_scenes, sizeof(BatchScene) * nscenes) != cudaSuccess ||
         cudaMalloc(&b->d_tasks, sizeof(BatchTask) * (ht.size() + 1)) != cudaSuccess ||
-        cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess)
+        cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&b->d_first, sizeof(int) * kBuildKinds * (nscenes + 1)) != cudaSuccess)
         rc = fail(RTG_NO_MEMORY, "batch tables");
     if (rc == RTG_OK && ht.size() &&
         cudaMemcpy(b->d_tasks, ht.data(), sizeof(BatchTask) * ht.size(), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -849,10 +896,15 @@ rtg_status rtg_batch_build_async(rtg_batch b, void* stream) {
     if (!b) return fail(RTG_INVALID_PARAM, "batch is NULL");
     CUDA_TRY(cudaSetDevice(b->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : b->scenes[0]->stream;
+    for (rtg_scene sc : b->scenes) {
+        rtg_status rc = ensure_cell_records(sc);
+        if (rc) return rc;
+        sc->crec_built = sc->tune.cell_records != 0;   // this build writes them
+    }
     rtg_status rc = batch_upload_build(b, st, false);
     if (rc == RTG_OK) rc = batch_upload_views(b, st, false);
     if (rc) return rc;
-    launch_build_batch(b->d_build, (int)b->scenes.size(), b->dims, st);
+    launch_build_batch(b->d_build, (int)b->scenes.size(), b->grid, b->bitmap_words, st);
     CUDA_TRY(cudaGetLastError());
     for (rtg_scene sc : b->scenes) sc->built = true;   // device status guards the traces
     return RTG_OK;
@@ -911,6 +963,7 @@ rtg_status rtg_batch_destroy(rtg_batch b) {
     cudaFree(b->d_scenes);
     cudaFree(b->d_tasks);
     cudaFree(b->d_counter);
+    cudaFree(b->d_first);
     delete b;
     return RTG_OK;
 }
@@ -924,6 +977,22 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
             return RTG_OK;
         case RTG_TUNE_PERSISTENT:
             s->tune.persistent = value ? 1 : 0;
+            return RTG_OK;
+        case RTG_TUNE_HEAVY_CELL:
+            if (value < 0) return fail(RTG_INVALID_PARAM, "heavy-cell threshold must be >= 0");
+            if (value > 0 && !s->d_defer) {
+                CUDA_TRY(cudaSetDevice(s->device));
+                if (cudaMalloc(&s->d_defer, sizeof(int32_t) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
+                    s->d_defer = nullptr;
+                    return fail(RTG_NO_MEMORY, "deferred-ray queues");
+                }
+            }
+            s->tune.heavy_cell = value;
+            return RTG_OK;
+        case RTG_TUNE_CELL_RECORDS:
+            // takes effect at the next build (which then also writes the records)
+            s->tune.cell_records = value ? 1 : 0;
+            if (!value) s->crec_built = false;
             return RTG_OK;
         default:
             return fail(RTG_INVALID_PARAM, "unknown tuning key");

@@ -29,6 +29,19 @@ namespace gridrt {
 
 static constexpr unsigned FULL = 0xffffffffu;
 
+// Batch launches use one flat grid: blocks [first[t], first[t+1]) work on
+// task t (first[] is a prefix table over the tasks' block counts).
+__device__ __forceinline__ int block_task(const int* __restrict__ first, int ntasks) {
+    int lo = 0, hi = ntasks - 1;
+    const int b = (int)blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(first + mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------------------
 // bbox + grid parameters
 // ---------------------------------------------------------------------------
@@ -36,11 +49,11 @@ static constexpr unsigned FULL = 0xffffffffu;
 // A NaN coordinate never wins a comparison there, so it is skipped here too.
 __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts, int64_t nverts,
                                                           BuildWork* w, GridParams* p, int32_t k, int64_t ntris,
-                                                          int64_t cell_cap) {
+                                                          int64_t cell_cap, unsigned vbx, unsigned vgx) {
     float mn0 = INFINITY, mn1 = INFINITY, mn2 = INFINITY;
     float mx0 = -INFINITY, mx1 = -INFINITY, mx2 = -INFINITY;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nverts; i += stride) {
+    const int64_t stride = (int64_t)vgx * blockDim.x;
+    for (int64_t i = (int64_t)vbx * blockDim.x + threadIdx.x; i < nverts; i += stride) {
         const float a = __ldg(verts + 3 * i), b = __ldg(verts + 3 * i + 1), c = __ldg(verts + 3 * i + 2);
         mn0 = a < mn0 ? a : mn0; mx0 = a > mx0 ? a : mx0;
         mn1 = b < mn1 ? b : mn1; mx1 = b > mx1 ? b : mx1;
@@ -81,7 +94,7 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
         atomicMax(&w->keys[5], f2key(mx2));
         __threadfence();
         const uint32_t ticket = atomicAdd(&w->ticket, 1u);
-        last = (ticket == gridDim.x - 1);
+        last = (ticket == vgx - 1);
     }
     __syncthreads();
     if (!last || threadIdx.x != 0) return;
@@ -145,9 +158,16 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) bbox_params_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap);
+__global__ void __launch_bounds__(256) bbox_params_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, blockIdx.x, gridDim.x);
+    }
 }
 
 static __device__ __forceinline__ bool fatal(uint32_t s) {
@@ -155,17 +175,17 @@ static __device__ __forceinline__ bool fatal(uint32_t s) {
 }
 
 __device__ __forceinline__ void zero_offsets_body(int32_t* __restrict__ offsets, uint32_t* __restrict__ occ,
-                                    const GridParams* __restrict__ p) {
+                                    const GridParams* __restrict__ p, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     if (occ) {
         const int64_t words = occ_words(p->res[0], p->res[1], p->res[2]);
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < words;
-             i += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t i = (int64_t)vbx * blockDim.x + threadIdx.x; i < words;
+             i += (int64_t)vgx * blockDim.x)
             occ[i] = 0u;
     }
     const int64_t n = p->ncells + 1;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x * 4;
-    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {
+    const int64_t stride = (int64_t)vgx * blockDim.x * 4;
+    for (int64_t i = ((int64_t)vbx * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {
         if (i + 4 <= n && ((i & 3) == 0)) {
             reinterpret_cast<int4*>(offsets)[i >> 2] = make_int4(0, 0, 0, 0);
         } else {
@@ -175,9 +195,16 @@ __device__ __forceinline__ void zero_offsets_body(int32_t* __restrict__ offsets,
 }
 
 template <bool MULTI>
-__global__ void zero_offsets_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    zero_offsets_body(a.offsets, a.occ, a.params);
+__global__ void zero_offsets_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        zero_offsets_body(a.offsets, a.occ, a.params, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        zero_offsets_body(a.offsets, a.occ, a.params, blockIdx.x, gridDim.x);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -289,13 +316,13 @@ __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restri
 
 __device__ __forceinline__ void count_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
                                                     int64_t ntris, GridParams* p, BuildWork* w,
-                                                    int32_t* __restrict__ counts, float4* __restrict__ tris) {
+                                                    int32_t* __restrict__ counts, float4* __restrict__ tris, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     Lite L;
     load_lite(p, L);
     const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
         warp_expand<true>(L, verts, idx, ntris, base, tris, p, w, [&](int32_t cell, int32_t, bool active) {
             const unsigned peers = __match_any_sync(FULL, cell);
@@ -306,20 +333,27 @@ __device__ __forceinline__ void count_body(const float* __restrict__ verts, cons
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) count_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris);
+__global__ void __launch_bounds__(256) count_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, blockIdx.x, gridDim.x);
+    }
 }
 
 __device__ __forceinline__ void scatter_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
                                                       int64_t ntris, GridParams* p, int32_t* __restrict__ cursor,
-                                                      int32_t* __restrict__ ids) {
+                                                      int32_t* __restrict__ ids, unsigned vbx, unsigned vgx) {
     if (p->status & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP)) return;
     Lite L;
     load_lite(p, L);
     const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
         const int64_t t = base + lane;
         int32_t lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
@@ -380,9 +414,16 @@ __device__ __forceinline__ void scatter_body(const float* __restrict__ verts, co
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    scatter_body(a.verts, a.idx, a.ntris, a.params, a.offsets, a.ids);
+__global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        scatter_body(a.verts, a.idx, a.ntris, a.params, a.offsets, a.ids, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        scatter_body(a.verts, a.idx, a.ntris, a.params, a.offsets, a.ids, blockIdx.x, gridDim.x);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -410,12 +451,12 @@ __device__ __forceinline__ int64_t block_sum_i64(int64_t v, int64_t* sh) {
 
 __device__ __forceinline__ void scan_reduce_body(const int32_t* __restrict__ counts,
                                                                    const GridParams* __restrict__ p,
-                                                                   int64_t* __restrict__ tile_sums) {
+                                                                   int64_t* __restrict__ tile_sums, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     const int64_t C = p->ncells;
     const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ int64_t sh[33];
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int64_t tile = vbx; tile < ntiles; tile += vgx) {
         const int64_t b = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
         int64_t s = 0;
 #pragma unroll
@@ -427,13 +468,20 @@ __device__ __forceinline__ void scan_reduce_body(const int32_t* __restrict__ cou
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    scan_reduce_body(a.offsets, a.params, a.tile_sums);
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        scan_reduce_body(a.offsets, a.params, a.tile_sums, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        scan_reduce_body(a.offsets, a.params, a.tile_sums, blockIdx.x, gridDim.x);
+    }
 }
 
 __device__ __forceinline__ void scan_tiles_body(GridParams* p, BuildWork* w, int64_t* __restrict__ tile_sums,
-                                                          int32_t* __restrict__ offsets, int64_t ref_cap) {
+                                                          int32_t* __restrict__ offsets, int64_t ref_cap, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     const int64_t C = p->ncells;
     const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
@@ -477,9 +525,16 @@ __device__ __forceinline__ void scan_tiles_body(GridParams* p, BuildWork* w, int
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(1024) scan_tiles_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    scan_tiles_body(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap);
+__global__ void __launch_bounds__(1024) scan_tiles_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        scan_tiles_body(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        scan_tiles_body(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap, blockIdx.x, gridDim.x);
+    }
 }
 
 // In-place inclusive scan of each tile plus its prefix; queues cells that
@@ -490,13 +545,13 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
                                                                  BuildWork* w, int32_t* __restrict__ q_small,
                                                                  int32_t* __restrict__ q_med,
                                                                  int32_t* __restrict__ q_large, int64_t q_small_cap,
-                                                                 int64_t q_med_cap, int64_t q_large_cap) {
+                                                                 int64_t q_med_cap, int64_t q_large_cap, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     const int64_t C = p->ncells;
     const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ int64_t sh[9];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    for (int64_t tile = vbx; tile < ntiles; tile += vgx) {
         const int64_t b = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
         int32_t v[SCAN_ITEMS];
         int64_t s = 0;
@@ -577,9 +632,16 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    scan_down_body(a.offsets, a.params, a.tile_sums, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap);
+__global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        scan_down_body(a.offsets, a.params, a.tile_sums, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        scan_down_body(a.offsets, a.params, a.tile_sums, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap, blockIdx.x, gridDim.x);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -591,12 +653,12 @@ static __device__ __forceinline__ bool sort_skip(const GridParams* p) {
 
 __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offsets, int32_t* __restrict__ ids,
                                                          const int32_t* __restrict__ q, const BuildWork* w,
-                                                         const GridParams* p) {
+                                                         const GridParams* p, unsigned vbx, unsigned vgx) {
     if (sort_skip(p)) return;
     const uint32_t nq = w->nsort[0];
     const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
     for (int64_t i = warp; i < nq; i += nwarps) {
         const int32_t c = q[i];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
@@ -616,20 +678,27 @@ __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offs
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    sort_small_body(a.offsets, a.ids, a.q_small, a.work, a.params);
+__global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        sort_small_body(a.offsets, a.ids, a.q_small, a.work, a.params, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        sort_small_body(a.offsets, a.ids, a.q_small, a.work, a.params, blockIdx.x, gridDim.x);
+    }
 }
 
 static constexpr int MED_MAX = 4096;
 
 __device__ __forceinline__ void sort_medium_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, const int32_t* __restrict__ q,
-                                                          const BuildWork* w, const GridParams* p) {
+                                                          const BuildWork* w, const GridParams* p, unsigned vbx, unsigned vgx) {
     if (sort_skip(p)) return;
     __shared__ int32_t a[MED_MAX];
     const uint32_t nq = w->nsort[1];
-    for (int64_t i = blockIdx.x; i < nq; i += gridDim.x) {
+    for (int64_t i = vbx; i < nq; i += vgx) {
         const int32_t c = q[i];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
         int m = 64;
@@ -655,9 +724,16 @@ __device__ __forceinline__ void sort_medium_body(const int32_t* __restrict__ off
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    sort_medium_body(a.offsets, a.ids, a.q_med, a.work, a.params);
+__global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        sort_medium_body(a.offsets, a.ids, a.q_med, a.work, a.params, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        sort_medium_body(a.offsets, a.ids, a.q_med, a.work, a.params, blockIdx.x, gridDim.x);
+    }
 }
 
 // Cells above 4096 entries: copy the list to scratch, then per id chunk set
@@ -665,7 +741,7 @@ __global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const B
 __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, int32_t* __restrict__ scratch,
                                                           const int32_t* __restrict__ q, const BuildWork* w,
-                                                          const GridParams* p, int32_t bitmap_words) {
+                                                          const GridParams* p, int32_t bitmap_words, unsigned vbx, unsigned vgx) {
     if (sort_skip(p)) return;
     extern __shared__ uint32_t bm[];
     __shared__ int32_t sh_min[32], sh_max[32];
@@ -673,7 +749,7 @@ __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offs
     __shared__ int32_t base_sh;
     const uint32_t nq = w->nsort[2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int64_t qi = blockIdx.x; qi < nq; qi += gridDim.x) {
+    for (int64_t qi = vbx; qi < nq; qi += vgx) {
         const int32_t c = q[qi];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
         int32_t mn = INT_MAX, mx = INT_MIN;
@@ -741,53 +817,98 @@ __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offs
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const BuildArgs* __restrict__ many) {
-    const BuildArgs& a = MULTI ? many[blockIdx.y] : one;
-    sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words);
+__global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
+                       int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+    } else {
+        const BuildArgs& a = one;
+        sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words, blockIdx.x, gridDim.x);
+    }
+}
+
+// Triangle records in cell-list order: crec[3i..3i+2] = tris[3 ids[i] ..].
+__device__ __forceinline__ void cell_records_body(const int32_t* __restrict__ ids, const float4* __restrict__ tris,
+                                                  float4* __restrict__ crec, const GridParams* p, unsigned vbx,
+                                                  unsigned vgx) {
+    if (!crec || build_failed(p->status)) return;
+    const int64_t R = p->nrefs;
+    const int64_t stride = (int64_t)vgx * blockDim.x;
+    for (int64_t i = (int64_t)vbx * blockDim.x + threadIdx.x; i < R; i += stride) {
+        const int64_t t = ids[i];
+        crec[3 * i] = __ldg(tris + 3 * t);
+        crec[3 * i + 1] = __ldg(tris + 3 * t + 1);
+        crec[3 * i + 2] = __ldg(tris + 3 * t + 2);
+    }
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(256) cell_records_kernel(BuildArgs one, const BuildArgs* __restrict__ many,
+                                                           const int* __restrict__ first, int ntasks) {
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        cell_records_body(a.ids, a.tris, a.crec, a.params, blockIdx.x - (unsigned)first[t],
+                          (unsigned)(first[t + 1] - first[t]));
+    } else {
+        cell_records_body(one.ids, one.tris, one.crec, one.params, blockIdx.x, gridDim.x);
+    }
 }
 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-// Enqueues the build.  Single scene: `one` is passed by value.  Batch:
-// `many` holds ntasks BuildArgs in device memory, block row y works on task y,
-// and `dims` carries the largest sizes over the tasks for the grid shapes.
-template <bool MULTI>
-static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BuildArgs& dims,
-                              cudaStream_t st) {
-    const int sms = dims.num_sms;
-    const unsigned ny = MULTI ? (unsigned)ntasks : 1u;
-    count_launches(dims.skip_bbox ? 9 : 10);
-    if (!dims.skip_bbox) {
-        int64_t blocks = (dims.nverts + 255) / 256;
-        blocks = blocks < 1 ? 1 : (blocks > 2 * sms ? 2 * sms : blocks);
-        bbox_params_kernel<MULTI><<<dim3((unsigned)blocks, ny), 256, 0, st>>>(one, many);
-    }
-    {
-        int64_t blocks = (dims.cell_cap / 4 + 255) / 256;
-        blocks = blocks < 1 ? 1 : (blocks > 8 * sms ? 8 * sms : blocks);
-        zero_offsets_kernel<MULTI><<<dim3((unsigned)blocks, ny), 256, 0, st>>>(one, many);
-    }
-    int64_t tri_blocks = (dims.ntris + 255) / 256;   // one warp per 32 triangles
-    tri_blocks = tri_blocks < 1 ? 1 : (tri_blocks > 16 * sms ? 16 * sms : tri_blocks);
-    count_kernel<MULTI><<<dim3((unsigned)tri_blocks, ny), 256, 0, st>>>(one, many);
-    int64_t tiles = (dims.cell_cap + SCAN_TILE - 1) / SCAN_TILE;
-    tiles = tiles < 1 ? 1 : (tiles > 8 * sms ? 8 * sms : tiles);
-    scan_reduce_kernel<MULTI><<<dim3((unsigned)tiles, ny), SCAN_THREADS, 0, st>>>(one, many);
-    scan_tiles_kernel<MULTI><<<dim3(1, ny), 1024, 0, st>>>(one, many);
-    scan_down_kernel<MULTI><<<dim3((unsigned)tiles, ny), SCAN_THREADS, 0, st>>>(one, many);
-    scatter_kernel<MULTI><<<dim3((unsigned)tri_blocks, ny), 256, 0, st>>>(one, many);
-    const unsigned per_task = MULTI ? (unsigned)((sms + ntasks - 1) / ntasks) : (unsigned)sms;
-    sort_small_kernel<MULTI><<<dim3(8 * per_task, ny), 256, 0, st>>>(one, many);
-    sort_medium_kernel<MULTI><<<dim3(2 * per_task, ny), 512, 0, st>>>(one, many);
-    sort_large_kernel<MULTI><<<dim3(per_task, ny), 1024, (size_t)dims.bitmap_words * 4, st>>>(one, many);
+// Block counts per kernel for one task; the single-scene launch uses them as
+// its grid sizes, the batch launch concatenates them per task.
+void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
+    auto clampi = [](int64_t v, int64_t hi) { return (int)(v < 1 ? 1 : (v > hi ? hi : v)); };
+    out[BK_BBOX] = clampi((a.nverts + 255) / 256, 2 * sms);
+    out[BK_ZERO] = clampi((a.cell_cap / 4 + 255) / 256, 8 * sms);
+    out[BK_TRI] = clampi((a.ntris + 255) / 256, 16 * sms);            // one warp per 32 triangles
+    out[BK_TILE] = clampi((a.cell_cap + SCAN_TILE - 1) / SCAN_TILE, 8 * sms);
+    out[BK_ONE] = 1;
+    out[BK_SSMALL] = clampi(a.cell_cap / 512 + 1, 8 * sms);
+    out[BK_SMED] = clampi(a.cell_cap / 8192 + 1, 2 * sms);
+    out[BK_SLARGE] = clampi(a.cell_cap / 65536 + 1, sms);
+    out[BK_REFS] = a.crec ? clampi((a.ref_cap + 255) / 256, 16 * sms) : 0;
 }
 
-void launch_build(const BuildArgs& a, cudaStream_t st) { launch_build_impl<false>(a, nullptr, 1, a, st); }
+template <bool MULTI>
+static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BatchGrid& g,
+                              bool skip_bbox, int bitmap_words, cudaStream_t st) {
+    count_launches(skip_bbox ? 9 : 10);
+    const int* f[kBuildKinds];
+    for (int k = 0; k < kBuildKinds; ++k) f[k] = MULTI ? g.first[k] : nullptr;
+    if (!skip_bbox) bbox_params_kernel<MULTI><<<g.total[BK_BBOX], 256, 0, st>>>(one, many, f[BK_BBOX], ntasks);
+    zero_offsets_kernel<MULTI><<<g.total[BK_ZERO], 256, 0, st>>>(one, many, f[BK_ZERO], ntasks);
+    count_kernel<MULTI><<<g.total[BK_TRI], 256, 0, st>>>(one, many, f[BK_TRI], ntasks);
+    scan_reduce_kernel<MULTI><<<g.total[BK_TILE], SCAN_THREADS, 0, st>>>(one, many, f[BK_TILE], ntasks);
+    scan_tiles_kernel<MULTI><<<g.total[BK_ONE], 1024, 0, st>>>(one, many, f[BK_ONE], ntasks);
+    scan_down_kernel<MULTI><<<g.total[BK_TILE], SCAN_THREADS, 0, st>>>(one, many, f[BK_TILE], ntasks);
+    scatter_kernel<MULTI><<<g.total[BK_TRI], 256, 0, st>>>(one, many, f[BK_TRI], ntasks);
+    sort_small_kernel<MULTI><<<g.total[BK_SSMALL], 256, 0, st>>>(one, many, f[BK_SSMALL], ntasks);
+    sort_medium_kernel<MULTI><<<g.total[BK_SMED], 512, 0, st>>>(one, many, f[BK_SMED], ntasks);
+    sort_large_kernel<MULTI><<<g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, st>>>(one, many, f[BK_SLARGE],
+                                                                                         ntasks);
+    if (g.total[BK_REFS] > 0) {
+        count_launches(1);
+        cell_records_kernel<MULTI><<<g.total[BK_REFS], 256, 0, st>>>(one, many, f[BK_REFS], ntasks);
+    }
+}
 
-void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BuildArgs& dims, cudaStream_t st) {
+void launch_build(const BuildArgs& a, cudaStream_t st) {
+    BatchGrid g{};
+    build_blocks(a, a.num_sms, g.total);
+    launch_build_impl<false>(a, nullptr, 1, g, a.skip_bbox, a.bitmap_words, st);
+}
+
+void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BatchGrid& g, int bitmap_words,
+                        cudaStream_t st) {
     if (ntasks <= 0) return;
-    launch_build_impl<true>(dims, d_tasks, ntasks, dims, st);
+    BuildArgs dummy{};
+    launch_build_impl<true>(dummy, d_tasks, ntasks, g, false, bitmap_words, st);
 }
 
 cudaError_t build_setup_attributes(int bitmap_words) {

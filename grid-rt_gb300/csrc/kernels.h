@@ -23,6 +23,7 @@ struct BuildArgs {
     uint32_t* occ;         // occupancy bitmap, cell_cap words (nullptr: not built)
     int64_t cell_cap;
     int32_t* ids;          // ref_cap entries
+    float4* crec;          // optional: 3 x ref_cap float4, triangle records in cell-list order
     int32_t* scratch;      // ref_cap entries
     int64_t ref_cap;
     int64_t* tile_sums;
@@ -39,10 +40,19 @@ void count_launches(int n);
 unsigned long long launches_so_far();
 
 void launch_build(const BuildArgs& a, cudaStream_t st);
-// Batch: ntasks BuildArgs in device memory (block row y builds task y); dims
-// holds the largest nverts / ntris / cell_cap over the tasks plus num_sms and
-// bitmap_words.
-void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BuildArgs& dims, cudaStream_t st);
+
+// Build kernels by work shape (grid sizing per task).
+enum BuildKind { BK_BBOX = 0, BK_ZERO, BK_TRI, BK_TILE, BK_ONE, BK_SSMALL, BK_SMED, BK_SLARGE, BK_REFS, kBuildKinds };
+// Per-task block counts of every build kernel (the single-scene grid sizes).
+void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]);
+// Batch launch: total[k] blocks for kernel kind k, first[k] a device prefix
+// table (ntasks + 1 ints) assigning blocks to tasks.
+struct BatchGrid {
+    int total[kBuildKinds];
+    const int* first[kBuildKinds];
+};
+void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BatchGrid& g, int bitmap_words,
+                        cudaStream_t st);
 // Host resolution of the grid parameters with the C library's powf (used when
 // the device flags ST_AMBIGUOUS); defined in api.cu.
 void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap);
@@ -56,6 +66,7 @@ struct SceneView {
     const int32_t* offsets;
     const int32_t* ids;
     const uint32_t* occ;
+    const float4* crec;    // records in cell-list order, or nullptr (then ids -> tris)
     const float4* tris;
 };
 
@@ -73,16 +84,25 @@ struct TraceCounters {
 struct TraceTuning {
     int empty_run = 8;     // empty cells a lane may walk per loop iteration: 4, 8 or 16
     int persistent = 1;    // 1: persistent warps over ray batches; 0: one batch per warp
+    int cell_records = 0;  // 1: the build also writes triangle records in cell-list order
+    int heavy_cell = 0;    // > 0: rays meeting a list longer than this finish in a warp-per-ray pass
 };
 
-// Trace launchers.  `counter` is a device word the launch zeroes and uses to
-// hand out ray batches; launches that may overlap need distinct counters.
+// Per-launch device state of a single-scene trace: three counters the launch
+// zeroes (ray claims, deferred rays, deferred claims) and the deferred-ray
+// queue; launches that may overlap need distinct slots.
+struct TraceSlot {
+    unsigned long long* ctr;
+    int32_t* defer;
+    int32_t defer_cap;
+};
+
 void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
-                          unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st);
+                          const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st);
 void launch_trace_any(const SceneView& s, const float4* rays, int64_t n, uint8_t* occ, TraceCounters* ctr,
-                      unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st);
+                      const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st);
 void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
-                         float4* shadow_rays, TraceCounters* ctr, unsigned long long* counter,
+                         float4* shadow_rays, TraceCounters* ctr, const TraceSlot& slot,
                          const TraceTuning& tune, int num_sms, cudaStream_t st, int diffuse = 0,
                          unsigned long long seed = 0);
 // Batched tracing: up to kMaxBatchScenes scenes, any number of tasks.

@@ -174,6 +174,7 @@ extern "C" rtg_status rtg_grid_build_noalloc(const float* d_verts, int64_t nvert
     a.tris = reinterpret_cast<float4*>(d_tri_records);
     a.offsets = d_offsets;
     a.occ = nullptr;   // the occupancy bitmap only serves the scene's trace kernels
+    a.crec = nullptr;
     a.cell_cap = offsets_cap < kMaxCells + 1 ? offsets_cap : kMaxCells + 1;
     a.ids = d_ids;
     a.scratch = reinterpret_cast<int32_t*>(d->arena + kOffScratch);

@@ -28,11 +28,14 @@ struct rtg_scene_s {
     int64_t cell_cap = 0;
     uint32_t* d_occ = nullptr;
     int64_t occ_cap = 0;
-    unsigned long long* d_ray_ctr = nullptr;   // ring of per-launch ray counters
+    unsigned long long* d_ray_ctr = nullptr;   // ring of per-launch counters, 4 words a slot
+    int32_t* d_defer = nullptr;                // ring of per-launch deferred-ray queues (tune.heavy_cell)
     unsigned ctr_seq = 0;
     gridrt::TraceTuning tune;
     int32_t* d_ids = nullptr;
     int64_t ids_cap = 0;
+    float4* d_crec = nullptr;            // cell-ordered triangle records (tune.cell_records)
+    int64_t crec_cap = 0;                // in float4
     int32_t* d_scratch = nullptr;
     int64_t scratch_cap = 0;
     int64_t* d_tiles = nullptr;
@@ -46,6 +49,7 @@ struct rtg_scene_s {
     int32_t bitmap_words = 32768;
 
     bool built = false;
+    bool crec_built = false;             // the last build wrote cell-ordered records
     int32_t k = 0;
     gridrt::GridParams hp{};   // host copy of the last successful build
 
@@ -56,8 +60,9 @@ struct rtg_scene_s {
 
 namespace gridrt {
 constexpr unsigned kRayCounters = 64;
+constexpr int32_t kDeferCap = 32768;    // deferred rays a launch can queue; more are traced in place
 // Read-only device view of a built scene (for the trace kernels).
 SceneView scene_view(rtg_scene s);
-// Next per-launch ray hand-out counter of the scene.
-unsigned long long* scene_counter(rtg_scene s);
+// Next per-launch counter slot (and deferred-ray queue) of the scene.
+TraceSlot scene_counter(rtg_scene s);
 }  // namespace gridrt

@@ -237,12 +237,14 @@ extern "C" rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, co
                     // one request through the single-scene kernels
                     const BatchTask& T = s.h_tasks[0];
                     rtg_scene sc = scenes[T.scene];
+                    TraceTuning t1 = sc->tune;
+                    t1.empty_run = tune.empty_run;
                     if (T.mode == RTG_MODE_ANY)
                         launch_trace_any(scene_view(sc), T.rays, T.n, static_cast<uint8_t*>(T.out), nullptr,
-                                         s.d_counter, tune, sc->num_sms, s.stream);
+                                         scene_counter(sc), t1, sc->num_sms, s.stream);
                     else
                         launch_trace_nearest(scene_view(sc), T.rays, T.n, static_cast<int4*>(T.out), nullptr,
-                                             s.d_counter, tune, sc->num_sms, s.stream);
+                                             scene_counter(sc), t1, sc->num_sms, s.stream);
                 } else {
                     cudaMemcpyAsync(s.d_tasks, s.h_tasks, sizeof(BatchTask) * ntasks, cudaMemcpyHostToDevice,
                                     s.stream);

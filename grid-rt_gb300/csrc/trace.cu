@@ -26,6 +26,8 @@
 namespace gridrt {
 
 static constexpr unsigned FULL = 0xffffffffu;
+static constexpr int32_t kDeferred = -3;    // Lane::id of a ray handed to the warp-per-ray pass
+static constexpr int32_t kNoHeavy = 0x7fffffff;
 
 static unsigned long long g_launches = 0;
 void count_launches(int n) { __atomic_add_fetch(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
@@ -63,17 +65,15 @@ __device__ __forceinline__ void load_sparams(const GridParams* __restrict__ gp, 
 struct Lane {
     float ox, oy, oz, dx, dy, dz;
     float ix, iy, iz;
-    float tnear, tmax, lo;
+    float tmax, lo;
     float tMx, tMy, tMz, tDx, tDy, tDz;
     int32_t x, y, z;
-    int32_t sx, sy, sz;      // steps (vr::sign of the direction)
-    int32_t ox_, oy_, oz_;   // out-of-grid limits (-1 or n)
     int32_t budget;
     float best;
     int32_t id;
     int32_t cw;          // cached occupancy word index
     uint32_t cword;      // its value
-    long long ray;       // ray index, -1 = none
+    int32_t ray;         // ray index within the launch or task, -1 = none
 };
 
 // Ray::update + AabbIntersection::clipRay + traverse3ddda set-up
@@ -100,7 +100,6 @@ __device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear
         rf = vmin(rf, vmax(tn, tf));
     }
     if (rn > rf) return false;
-    L.tnear = rn;
     L.lo = fsub(rn, kHitEpsilon);
     const int32_t sx = __float_as_uint(L.dx) >> 31, sy = __float_as_uint(L.dy) >> 31, sz = __float_as_uint(L.dz) >> 31;
     L.x = vclamp(world_to_voxel(fadd(L.ox, fmul(L.dx, rn)), P.bmin[0], P.inv[0]), 0, P.res[0] - 1);
@@ -112,12 +111,6 @@ __device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear
     L.tMx = fmul(fsub(voxel_to_world(L.x + (sx ^ 1), P.cell[0], P.bmin[0]), L.ox), L.ix);
     L.tMy = fmul(fsub(voxel_to_world(L.y + (sy ^ 1), P.cell[1], P.bmin[1]), L.oy), L.iy);
     L.tMz = fmul(fsub(voxel_to_world(L.z + (sz ^ 1), P.cell[2], P.bmin[2]), L.oz), L.iz);
-    L.sx = L.dx < 0.0f ? -1 : (L.dx > 0.0f ? 1 : 0);
-    L.sy = L.dy < 0.0f ? -1 : (L.dy > 0.0f ? 1 : 0);
-    L.sz = L.dz < 0.0f ? -1 : (L.dz > 0.0f ? 1 : 0);
-    L.ox_ = sx ? -1 : P.res[0];
-    L.oy_ = sy ? -1 : P.res[1];
-    L.oz_ = sz ? -1 : P.res[2];
     // A walk visits at most nx+ny+nz-2 cells; the bound only guards against a
     // zero direction component (outside the reference's domain) looping.
     L.budget = P.res[0] + P.res[1] + P.res[2] + 3;
@@ -128,21 +121,25 @@ __device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear
 }
 
 // One DDA step (src/rtplugins/UniformGridAccStruct.cpp:179-195): the strict-<
-// axis choice, then the exit test x != outX && y != outY && z != outZ with
-// out = -1 for a negative direction sign bit, n otherwise (:137-139).  True
-// when the walk has left the grid.
+// axis choice and a step of vr::sign(direction).  The reference then exits
+// when x == outX (or y, z), with out = -1 for a negative direction sign bit and
+// n otherwise (:137-139, :195).  A walk starts inside the grid and moves each
+// coordinate only toward its out value, so it reaches out exactly when the
+// coordinate leaves [0, n): the test below is the same predicate.  True when
+// the walk has left the grid.
 __device__ __forceinline__ bool dda_step(const SParams& P, Lane& L) {
     if (L.tMx < L.tMy && L.tMx < L.tMz) {
-        L.x += L.sx;
+        L.x += L.dx < 0.0f ? -1 : (L.dx > 0.0f ? 1 : 0);
         L.tMx = fadd(L.tMx, L.tDx);
     } else if (L.tMy < L.tMz) {
-        L.y += L.sy;
+        L.y += L.dy < 0.0f ? -1 : (L.dy > 0.0f ? 1 : 0);
         L.tMy = fadd(L.tMy, L.tDy);
     } else {
-        L.z += L.sz;
+        L.z += L.dz < 0.0f ? -1 : (L.dz > 0.0f ? 1 : 0);
         L.tMz = fadd(L.tMz, L.tDz);
     }
-    return !(L.x != L.ox_ && L.y != L.oy_ && L.z != L.oz_) || --L.budget <= 0;
+    return (unsigned)L.x >= (unsigned)P.res[0] || (unsigned)L.y >= (unsigned)P.res[1] ||
+           (unsigned)L.z >= (unsigned)P.res[2] || --L.budget <= 0;
 }
 
 // Moller-Trumbore test of one triangle record against the lane's ray with the
@@ -177,7 +174,8 @@ __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, 
 template <int MODE, int ER>
 __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t* __restrict__ offsets,
                                         const int32_t* __restrict__ ids, const float4* __restrict__ tris,
-                                        const uint32_t* __restrict__ occ, uint32_t& cells, uint32_t& tests) {
+                                        const uint32_t* __restrict__ occ, const float4* __restrict__ crec,
+                                        int32_t heavy, uint32_t& cells, uint32_t& tests) {
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
     for (int s = 0; s < ER; ++s) {
         ++cells;
@@ -189,9 +187,33 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
         if (L.cword & occ_bit(L.x, L.y, L.z)) {
             const int32_t c = L.x + L.y * nx + L.z * nxy;
             const int32_t b = __ldg(offsets + c), e = __ldg(offsets + c + 1);
+            if (e - b > heavy) {
+                // long list: the ray goes to the warp-per-ray pass, which
+                // walks it again from the start (this cell is not counted)
+                --cells;
+                L.id = kDeferred;
+                return true;
+            }
             const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
             tests += (uint32_t)(e - b);
             int32_t i = b;
+            if (crec) {
+                // records stored in cell-list order: no id indirection
+                for (; i + 1 < e; i += 2) {
+                    const float4 A0 = __ldg(crec + 3 * (int64_t)i), B0 = __ldg(crec + 3 * (int64_t)i + 1),
+                                 C0 = __ldg(crec + 3 * (int64_t)i + 2);
+                    const float4 A1 = __ldg(crec + 3 * (int64_t)i + 3), B1 = __ldg(crec + 3 * (int64_t)i + 4),
+                                 C1 = __ldg(crec + 3 * (int64_t)i + 5);
+                    if (test_tri<MODE>(L, __float_as_int(A0.w), A0, B0, C0, hi)) return true;
+                    if (test_tri<MODE>(L, __float_as_int(A1.w), A1, B1, C1, hi)) return true;
+                }
+                if (i < e) {
+                    const float4 A0 = __ldg(crec + 3 * (int64_t)i), B0 = __ldg(crec + 3 * (int64_t)i + 1),
+                                 C0 = __ldg(crec + 3 * (int64_t)i + 2);
+                    if (test_tri<MODE>(L, __float_as_int(A0.w), A0, B0, C0, hi)) return true;
+                }
+                i = e;
+            }
             for (; i + 1 < e; i += 2) {
                 const int32_t t0 = __ldg(ids + i), t1 = __ldg(ids + i + 1);
                 const float4 A0 = __ldg(tris + 3 * (int64_t)t0), B0 = __ldg(tris + 3 * (int64_t)t0 + 1),
@@ -208,7 +230,8 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
                 if (test_tri<MODE>(L, t0, A0, B0, C0, hi)) return true;
             }
             if (L.best < kFltMax) {
-                if (MODE == MODE_ANY) L.id = -1;   // first cell with a hit decides: not before tmax
+                // any-hit: the first cell with a hit decides -- here not before tmax
+                if (MODE == MODE_ANY) L.id = -1;
                 return true;
             }
             if (dda_step(P, L)) {
@@ -262,9 +285,9 @@ __device__ __forceinline__ int4 refined_hit(const float4* __restrict__ tris, con
     return make_int4(L.id, __float_as_int(tt), __float_as_int(u), __float_as_int(v));
 }
 
-__device__ __forceinline__ void ray_pixel(long long i, const CameraArgs& cam, int32_t& px, int32_t& py) {
+__device__ __forceinline__ void ray_pixel(int32_t i, const CameraArgs& cam, int32_t& px, int32_t& py) {
     if (cam.order == 1) {
-        const long long tile = i >> 6;
+        const int32_t tile = i >> 6;
         const int32_t r = (int32_t)(i & 63);
         const int32_t tiles_x = cam.width >> 3;
         const int32_t tx = (int32_t)(tile % tiles_x), ty = (int32_t)(tile / tiles_x);
@@ -287,14 +310,17 @@ struct TraceIO {
     int diffuse;              // CAMERA: secondary = cosine-weighted diffuse ray
     unsigned long long seed;
     long long n;
-    unsigned long long* counter;
+    unsigned long long* counter;   // [0] ray claims, [1] deferred rays, [2] deferred claims
     TraceCounters* ctr;
+    int32_t* defer;                // deferred ray indices (nullptr: no deferral)
+    int32_t defer_cap;
+    int32_t heavy;                 // lists longer than this are deferred (kNoHeavy: never)
 };
 
 // Loads ray `r` into the lane; false when the ray ends at once (misses the
 // grid, or ANY mode with no shadow ray).
 template <int MODE>
-__device__ __forceinline__ bool start_ray(const SParams& P, const TraceIO& io, Lane& L, long long r) {
+__device__ __forceinline__ bool start_ray(const SParams& P, const TraceIO& io, Lane& L, int32_t r) {
     float tnear, tfar;
     if (MODE == MODE_CAMERA) {
         int32_t px, py;
@@ -308,7 +334,7 @@ __device__ __forceinline__ bool start_ray(const SParams& P, const TraceIO& io, L
         tnear = kRayEpsilon;
         tfar = kFltMax;
     } else {
-        const float4 a = __ldg(io.rays + 2 * r), b = __ldg(io.rays + 2 * r + 1);
+        const float4 a = __ldg(io.rays + 2 * (int64_t)r), b = __ldg(io.rays + 2 * (int64_t)r + 1);
         L.ox = a.x; L.oy = a.y; L.oz = a.z;
         L.dx = b.x; L.dy = b.y; L.dz = b.z;
         tnear = a.w;
@@ -350,20 +376,20 @@ __device__ __forceinline__ float3 cosine_dir(float nx, float ny, float nz, unsig
     return make_float3(lx * tx + ly * bx + lz * nx, lx * ty + ly * by + lz * ny, lx * tz + ly * bz + lz * nz);
 }
 
+// Writes the lane's result.  Returns true when the lane goes on with a
+// follow-up ray (no mode does so today; the trace loop supports it).
 template <int MODE>
-__device__ __forceinline__ void finish_ray(const TraceIO& io, const float4* __restrict__ tris, const Lane& L) {
-    const long long r = L.ray;
+__device__ __forceinline__ bool finish_ray(const TraceIO& io, const SParams& P, const float4* __restrict__ tris,
+                                           Lane& L) {
+    const int64_t r = L.ray;
     if (MODE == MODE_ANY) {
         io.occ[r] = L.id == -2 ? 2 : (L.id >= 0 ? 1 : 0);
-        return;
+        return false;
     }
     int4 h = make_int4(-1, 0, 0, 0);
     if (L.id >= 0) h = refined_hit(tris, L);
     io.hits[r] = h;
-    if (MODE == MODE_CAMERA && io.shadow_rays) {
-        // Sample::computeHitPosition, flat normal facing the ray, initLightRay
-        // offset and initShadowRay (src/rtcore/Sample.cpp:22-42,177-180,224-236),
-        // SimplePointLight::illuminate (src/rtplugins/SimplePointLight.cpp:25-33)
+    if (MODE == MODE_CAMERA) {
         float4 sa = make_float4(0.f, 0.f, 0.f, kRayEpsilon), sb = make_float4(0.f, 0.f, 0.f, -1.0f);
         if (L.id >= 0 && io.diffuse) {
             // secondary diffuse ray from the hit point, offset along the
@@ -380,6 +406,9 @@ __device__ __forceinline__ void finish_ray(const TraceIO& io, const float4* __re
                              L.oz + L.dz * t + nz * kRayEpsilon, kRayEpsilon);
             sb = make_float4(w.x, w.y, w.z, kFltMax);
         } else if (L.id >= 0 && io.has_light) {
+            // Sample::computeHitPosition, flat normal facing the ray, initLightRay
+            // offset and initShadowRay (src/rtcore/Sample.cpp:22-42,177-180,224-236),
+            // SimplePointLight::illuminate (src/rtplugins/SimplePointLight.cpp:25-33)
             const float t = __int_as_float(h.y);
             const float4 B = __ldg(tris + 3 * (int64_t)L.id + 1);
             const float4 C = __ldg(tris + 3 * (int64_t)L.id + 2);
@@ -396,31 +425,58 @@ __device__ __forceinline__ void finish_ray(const TraceIO& io, const float4* __re
                 sb = make_float4(lx, ly, lz, 1.0f);
             }
         }
-        io.shadow_rays[2 * r] = sa;
-        io.shadow_rays[2 * r + 1] = sb;
+        if (io.shadow_rays) {
+            io.shadow_rays[2 * r] = sa;
+            io.shadow_rays[2 * r + 1] = sb;
+        }
     }
+    return false;
 }
 
-// Traces the 32 rays [base, base + 32) of `io` (one per lane) to the end.
 template <int MODE, int ER>
 __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView& s, const TraceIO& io, Lane& L,
                                               long long base, uint32_t& cells, uint32_t& tests, uint32_t& started) {
     const int lane = threadIdx.x & 31;
-    L.ray = base + lane;
-    bool active = L.ray < io.n;
+    const long long ray = base + lane;
+    bool active = ray < io.n;
+    L.ray = (int32_t)ray;
+    int32_t heavy = io.heavy;
+    const uint32_t cells0 = cells, tests0 = tests;
     if (active) {
         ++started;
         if (!start_ray<MODE>(P, io, L, L.ray)) {
             if (L.id != -2) L.id = -1;
-            finish_ray<MODE>(io, s.tris, L);
-            active = false;
+            active = finish_ray<MODE>(io, P, s.tris, L);
         }
     }
     while (__any_sync(FULL, active)) {
-        if (active && advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, cells, tests)) {
-            finish_ray<MODE>(io, s.tris, L);
-            active = false;
+        bool fin = active && advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, s.crec, heavy, cells, tests);
+        if (io.defer) {
+            // warp-aggregated push of the lanes that met a long list
+            const bool d = fin && L.id == kDeferred;
+            const unsigned m = __ballot_sync(FULL, d);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                unsigned long long at = 0;
+                if (lane == leader) at = atomicAdd(io.counter + 1, (unsigned long long)__popc(m));
+                at = __shfl_sync(FULL, at, leader);
+                if (d) {
+                    const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
+                    if (slot < (unsigned long long)io.defer_cap) {
+                        io.defer[slot] = L.ray;
+                        cells = cells0;          // the warp-per-ray pass counts this ray
+                        tests = tests0;
+                        --started;
+                        active = false;
+                    } else {
+                        heavy = kNoHeavy;        // queue full: the lane tests the cell itself
+                        L.id = -1;
+                    }
+                    fin = false;
+                }
+            }
         }
+        if (fin) active = finish_ray<MODE>(io, P, s.tris, L);
     }
 }
 
@@ -438,8 +494,14 @@ __device__ __forceinline__ void flush_counters(TraceCounters* ctr, uint32_t star
     }
 }
 
+// Eight blocks of 128 threads per SM (64 registers a thread): the walk is
+// latency-bound, and resident warps matter more than the few spilled words.
+#ifndef GRIDRT_TRACE_MIN_BLOCKS
+#define GRIDRT_TRACE_MIN_BLOCKS 8
+#endif
+
 template <int MODE, bool COUNT, int ER>
-__global__ void __launch_bounds__(128) trace_kernel(SceneView s, TraceIO io) {
+__global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(SceneView s, TraceIO io) {
     __shared__ SParams P;
     load_sparams(s.params, P);
     const int lane = threadIdx.x & 31;
@@ -454,6 +516,82 @@ __global__ void __launch_bounds__(128) trace_kernel(SceneView s, TraceIO io) {
         trace_batch32<MODE, ER>(P, s, io, L, (long long)b, cells, tests, started);
     }
     if (COUNT) flush_counters(io.ctr, started, cells, tests);
+}
+
+// Warp-per-ray pass over the deferred rays: all 32 lanes hold the same ray
+// and walk the same cells; a cell's list is split over the lanes (lane j
+// tests entries j, j+32, ...), each lane keeping the first minimum of its
+// share, and the warp takes the minimum t, ties to the smaller triangle id.
+// Lists are sorted by id, so that is the first minimum in list order: the
+// one-lane walk's result.  ANY rays are occluded when that minimum is below
+// tmax -- also the one-lane walk's rule, which accepts every new minimum and
+// stops at the first below tmax.
+template <int MODE, bool COUNT>
+__global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io) {
+    __shared__ SParams P;
+    load_sparams(s.params, P);
+    const int lane = threadIdx.x & 31;
+    unsigned long long nd = io.counter[1];
+    if (nd > (unsigned long long)io.defer_cap) nd = (unsigned long long)io.defer_cap;
+    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
+    uint32_t cells = 0, tests = 0;
+    for (;;) {
+        unsigned long long j = 0;
+        if (lane == 0) j = atomicAdd(io.counter + 2, 1ull);
+        j = __shfl_sync(FULL, j, 0);
+        if (j >= nd) break;
+        Lane L;
+        L.ray = __ldg(io.defer + j);
+        bool done = !start_ray<MODE>(P, io, L, L.ray);
+        if (done && L.id != -2) L.id = -1;
+        while (!done) {
+            ++cells;
+            const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+            if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
+                const int32_t c = L.x + L.y * nx + L.z * nxy;
+                const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
+                const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+                tests += (uint32_t)(e - b);
+                for (int32_t i = b + lane; i < e; i += 32) {
+                    int32_t tid;
+                    float4 A, B, C;
+                    if (s.crec) {
+                        A = __ldg(s.crec + 3 * (int64_t)i);
+                        B = __ldg(s.crec + 3 * (int64_t)i + 1);
+                        C = __ldg(s.crec + 3 * (int64_t)i + 2);
+                        tid = __float_as_int(A.w);
+                    } else {
+                        tid = __ldg(s.ids + i);
+                        A = __ldg(s.tris + 3 * (int64_t)tid);
+                        B = __ldg(s.tris + 3 * (int64_t)tid + 1);
+                        C = __ldg(s.tris + 3 * (int64_t)tid + 2);
+                    }
+                    test_tri<MODE_NEAREST>(L, tid, A, B, C, hi);
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ot = __shfl_xor_sync(FULL, L.best, o);
+                    const int32_t oid = __shfl_xor_sync(FULL, L.id, o);
+                    if (ot < L.best || (ot == L.best && (uint32_t)oid < (uint32_t)L.id)) {
+                        L.best = ot;
+                        L.id = oid;
+                    }
+                }
+                if (L.best < kFltMax) {
+                    if (MODE == MODE_ANY && !(L.best < L.tmax)) L.id = -1;
+                    done = true;
+                }
+            }
+            if (!done && dda_step(P, L)) {
+                L.id = -1;
+                done = true;
+            }
+        }
+        if (lane == 0) finish_ray<MODE>(io, P, s.tris, L);
+    }
+    if (COUNT) {
+        if (lane != 0) cells = tests = 0;
+        flush_counters(io.ctr, 0, cells, tests);
+    }
 }
 
 // Many (scene, ray batch) tasks in one persistent launch.  Task t owns the
@@ -485,6 +623,7 @@ __global__ void __launch_bounds__(128) trace_batch_kernel(const BatchScene* __re
         TraceIO io{};
         io.rays = T.rays;
         io.n = T.n;
+        io.heavy = kNoHeavy;
         const long long base = (long long)b - T.first;
         if (T.mode == MODE_ANY) {
             io.occ = static_cast<uint8_t*>(T.out);
@@ -534,40 +673,59 @@ static void launch_count(const SceneView& s, const TraceIO& io, const TraceTunin
     else launch_er<MODE, COUNT, 16>(s, io, tune, num_sms, st);
 }
 
+template <int MODE, bool COUNT>
+static void launch_wide(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_kernel<MODE, COUNT>, 128, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    trace_wide_kernel<MODE, COUNT><<<per_sm * num_sms, 128, 0, st>>>(s, io);
+}
+
 template <int MODE>
-static void launch_mode(const SceneView& s, TraceIO io, const TraceTuning& tune, int num_sms, cudaStream_t st) {
-    count_launches(1);
-    cudaMemsetAsync(io.counter, 0, sizeof(unsigned long long), st);
+static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, const TraceTuning& tune, int num_sms,
+                        cudaStream_t st) {
+    const bool defer = tune.heavy_cell > 0 && slot.defer && slot.defer_cap > 0;
+    io.counter = slot.ctr;
+    io.defer = defer ? slot.defer : nullptr;
+    io.defer_cap = defer ? slot.defer_cap : 0;
+    io.heavy = defer ? tune.heavy_cell : kNoHeavy;
+    count_launches(defer ? 2 : 1);
+    cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
+    if (defer) {
+        if (io.ctr) launch_wide<MODE, true>(s, io, num_sms, st);
+        else launch_wide<MODE, false>(s, io, num_sms, st);
+    }
 }
 
 void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
-                          unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+                          const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     if (n <= 0) return;
     TraceIO io{};
     io.rays = rays;
     io.hits = hits;
     io.n = n;
-    io.counter = counter;
     io.ctr = ctr;
-    launch_mode<MODE_NEAREST>(s, io, tune, num_sms, st);
+    launch_mode<MODE_NEAREST>(s, io, slot, tune, num_sms, st);
 }
 
 void launch_trace_any(const SceneView& s, const float4* rays, int64_t n, uint8_t* occ, TraceCounters* ctr,
-                      unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+                      const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     if (n <= 0) return;
     TraceIO io{};
     io.rays = rays;
     io.occ = occ;
     io.n = n;
-    io.counter = counter;
     io.ctr = ctr;
-    launch_mode<MODE_ANY>(s, io, tune, num_sms, st);
+    launch_mode<MODE_ANY>(s, io, slot, tune, num_sms, st);
 }
 
 void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
-                         float4* shadow_rays, TraceCounters* ctr, unsigned long long* counter,
+                         float4* shadow_rays, TraceCounters* ctr, const TraceSlot& slot,
                          const TraceTuning& tune, int num_sms, cudaStream_t st, int diffuse,
                          unsigned long long seed) {
     const int64_t n = (int64_t)cam.width * cam.height;
@@ -581,9 +739,8 @@ void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, 
     io.light = light ? make_float3(light[0], light[1], light[2]) : make_float3(0.f, 0.f, 0.f);
     io.has_light = light != nullptr;
     io.n = n;
-    io.counter = counter;
     io.ctr = ctr;
-    launch_mode<MODE_CAMERA>(s, io, tune, num_sms, st);
+    launch_mode<MODE_CAMERA>(s, io, slot, tune, num_sms, st);
 }
 
 template <int ER>

@@ -65,7 +65,34 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode:
             print(" ".join(cmd), r.stdout, r.stderr)
             raise RuntimeError("link failed")
+    build_tools()
     return LIB
+
+
+TOOLS = {
+    # C++ driver of the plugin mirror (include/gridrt_rtp.hpp), used by tests
+    "rtp_adapter_check": os.path.join(REPO, "tests", "cpp", "rtp_adapter_check.cpp"),
+}
+
+
+def tool_path(name: str) -> str:
+    return os.path.join(OUT_DIR, name)
+
+
+def build_tools() -> None:
+    for name, src in TOOLS.items():
+        out = tool_path(name)
+        if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(src), os.path.getmtime(LIB),
+                                                                   _newest(glob.glob(os.path.join(INCLUDE, "*")))):
+            continue
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64") \
+            if os.path.isabs(nvcc()) else "/usr/local/cuda/lib64"
+        cmd = ["g++", "-O2", "-std=c++17", "-I", INCLUDE, src, "-o", out, "-L", OUT_DIR, "-lgridrt",
+               f"-Wl,-rpath,{OUT_DIR}", "-L", cuda_lib, "-lcudart", f"-Wl,-rpath,{cuda_lib}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            print(" ".join(cmd), r.stdout, r.stderr)
+            raise RuntimeError(f"building {name} failed")
 
 
 if __name__ == "__main__":

@@ -24,6 +24,8 @@ RTG_INVALID_GEOMETRY = 7
 RTG_TRACE_COUNTERS = 1
 RTG_TUNE_EMPTY_RUN = 1
 RTG_TUNE_PERSISTENT = 2
+RTG_TUNE_CELL_RECORDS = 3
+RTG_TUNE_HEAVY_CELL = 4
 ORDER = {"scanline": 0, "morton8": 1}
 
 
@@ -96,7 +98,9 @@ EXPORTS = [
 
 
 def lib_path() -> str:
-    return _build.LIB
+    """The in-tree library; GRIDRT_LIB names another build of the same
+    sources (e.g. one compiled with different -D options)."""
+    return os.environ.get("GRIDRT_LIB") or _build.LIB
 
 
 def load(build_if_missing: bool = True):
@@ -167,9 +171,11 @@ def check(rc: int):
 
 
 def _ptr(a) -> int:
-    """Address of a numpy array or torch tensor."""
+    """Address of a numpy array or torch tensor (an int is taken as an address)."""
     if a is None:
         return None
+    if isinstance(a, int):
+        return a
     if hasattr(a, "data_ptr"):
         return a.data_ptr()
     return a.ctypes.data
@@ -308,11 +314,16 @@ class Scene:
         check(load().rtg_trace_frame(self.h, C.byref(cs), _ptr(self._light), _ptr(hits_host), _ptr(occ_host),
                                      stream))
 
-    def set_tuning(self, empty_run: int = None, persistent: bool = None):
+    def set_tuning(self, empty_run: int = None, persistent: bool = None, cell_records: bool = None,
+                   heavy_cell: int = None):
         if empty_run is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_PERSISTENT, 1 if persistent else 0))
+        if cell_records is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_CELL_RECORDS, 1 if cell_records else 0))
+        if heavy_cell is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_HEAVY_CELL, int(heavy_cell)))
 
     def counters(self, reset: bool = True):
         out = (C.c_int64 * 3)()

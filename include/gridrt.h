@@ -189,8 +189,11 @@ rtg_status rtg_trace_camera_device(rtg_scene scene, const rtg_camera* cam, rtg_h
  * path; it feeds the skewed-density workload's secondary rays. */
 rtg_status rtg_trace_camera_diffuse_device(rtg_scene scene, const rtg_camera* cam, uint64_t seed, rtg_hit* d_hits,
                                            float* d_secondary_rays, int32_t flags, void* stream);
-/* Primary + shadow frame: camera closest hits, shadow rays and any-hit in one
- * call on the device.  occluded[i]: 0 lit, 1 shadowed, 2 no shadow ray. */
+/* Primary + shadow frame: camera closest hits, then every hit's shadow ray
+ * traced with the any-hit rules (two launches).  occluded[i]: 0 lit,
+ * 1 shadowed, 2 no shadow ray.  d_shadow_rays (optional, may be NULL: the
+ * scene's staging buffer is used) receives the shadow rays as
+ * rtg_trace_camera_device writes them. */
 rtg_status rtg_trace_frame_device(rtg_scene scene, const rtg_camera* cam, const float* light_pos,
                                   rtg_hit* d_hits, uint8_t* d_occluded, float* d_shadow_rays, void* stream);
 
@@ -298,8 +301,13 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
 
 /* Trace launch shape for this scene (results never depend on it):
  *   RTG_TUNE_EMPTY_RUN   empty cells a ray may walk per loop turn: 4, 8, 16 (default 8)
- *   RTG_TUNE_PERSISTENT  1: persistent warps claim ray batches (default); 0: one batch per warp */
-enum { RTG_TUNE_EMPTY_RUN = 1, RTG_TUNE_PERSISTENT = 2 };
+ *   RTG_TUNE_PERSISTENT  1: persistent warps claim ray batches (default); 0: one batch per warp
+ *   RTG_TUNE_CELL_RECORDS 1: builds also store the triangle records in cell-list order
+ *                        (48 B per reference) so traces skip the id indirection; from the next build
+ *   RTG_TUNE_HEAVY_CELL  n > 0: a ray that meets a cell list longer than n is finished by a
+ *                        second pass that traces it with a whole warp (the list split over
+ *                        32 lanes); 0 (default) off.  Results are identical either way. */
+enum { RTG_TUNE_EMPTY_RUN = 1, RTG_TUNE_PERSISTENT = 2, RTG_TUNE_CELL_RECORDS = 3, RTG_TUNE_HEAVY_CELL = 4 };
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 
 /* Counters accumulated by calls made with RTG_TRACE_COUNTERS since the last

@@ -1,0 +1,88 @@
+// Drives the C++ plugin mirror (include/gridrt_rtp.hpp) the way the
+// reference's Context does: build a Geometry through the builder, then trace
+// rays one by one through the virtual per-ray calls and in one batch.
+// Reads rays and geometry from binary files, writes hits for the Python test.
+//   rtp_adapter_check <verts.f32> <tris.i32> <rays.f32> <out_prefix>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <vector>
+
+#include "gridrt_rtp.hpp"
+
+using namespace gridrt;
+
+template <class T>
+static std::vector<T> load(const char* path) {
+    std::ifstream f(path, std::ios::binary | std::ios::ate);
+    std::vector<T> v((size_t)f.tellg() / sizeof(T));
+    f.seekg(0);
+    f.read(reinterpret_cast<char*>(v.data()), (std::streamsize)(v.size() * sizeof(T)));
+    return v;
+}
+
+int main(int argc, char** argv) {
+    if (argc != 5) return 2;
+    std::vector<float> verts = load<float>(argv[1]);
+    std::vector<int32_t> tris = load<int32_t>(argv[2]);
+    std::vector<float> rays = load<float>(argv[3]);
+    rt::Geometry g;
+    for (size_t i = 0; i + 2 < verts.size(); i += 3) g.vertices.emplace_back(verts[i], verts[i + 1], verts[i + 2]);
+    for (size_t t = 0; t + 2 < tris.size(); t += 3) g.triDesc.push_back({{(uint32_t)tris[t], (uint32_t)tris[t + 1], (uint32_t)tris[t + 2]}});
+    rtp::UniformGridAccStructBuilder builder(4);
+    builder.buildGeometry(&g);
+    if (builder.lastStatus() != RTG_OK) {
+        std::fprintf(stderr, "build failed: %s\n", rtg_last_error());
+        return 1;
+    }
+    auto* acc = static_cast<rtp::UniformGridAccStruct*>(g.accStruct.get());
+    rt::Instance inst;
+    inst.geometry = &g;
+    const size_t n = rays.size() / 8;
+    std::vector<rt::Ray> rv(n);
+    for (size_t i = 0; i < n; ++i) {
+        const float* q = &rays[8 * i];
+        rv[i].orig = rt::vec3f(q[0], q[1], q[2]);
+        rv[i].tnear = q[3];
+        rv[i].dir = rt::vec3f(q[4], q[5], q[6]);
+        rv[i].tfar = q[7];
+    }
+    // per-ray virtual calls (as IAccStruct::traceNearestInstance makes them)
+    std::vector<float> single(4 * n), batch(4 * n);
+    std::vector<uint8_t> any_single(n);
+    rt::IAccStruct* base = acc;
+    for (size_t i = 0; i < n; ++i) {
+        rt::Ray r = rv[i];
+        rt::Hit h;
+        base->traceNearestGeometry(inst, r, h);
+        int32_t id = h.instance ? (int32_t)h.triangleId : -1;
+        std::memcpy(&single[4 * i], &id, 4);
+        single[4 * i + 1] = h.instance ? h.distance : 0.f;
+        single[4 * i + 2] = h.instance ? h.v1Coord : 0.f;
+        single[4 * i + 3] = h.instance ? h.v2Coord : 0.f;
+        rt::Ray r2 = rv[i];
+        any_single[i] = base->traceAnyGeometry(inst, r2, h) ? 1 : 0;
+    }
+    std::vector<rt::Hit> hits;
+    acc->traceNearestBatch(inst, rv, hits);
+    for (size_t i = 0; i < n; ++i) {
+        int32_t id = hits[i].instance ? (int32_t)hits[i].triangleId : -1;
+        std::memcpy(&batch[4 * i], &id, 4);
+        batch[4 * i + 1] = hits[i].instance ? hits[i].distance : 0.f;
+        batch[4 * i + 2] = hits[i].instance ? hits[i].v1Coord : 0.f;
+        batch[4 * i + 3] = hits[i].instance ? hits[i].v2Coord : 0.f;
+    }
+    std::vector<uint8_t> any_batch;
+    acc->traceAnyBatch(rv, any_batch);
+    auto save = [&](const char* suffix, const void* data, size_t bytes) {
+        std::string path = std::string(argv[4]) + suffix;
+        std::ofstream(path, std::ios::binary).write(static_cast<const char*>(data), (std::streamsize)bytes);
+    };
+    save(".single.f32", single.data(), single.size() * 4);
+    save(".batch.f32", batch.data(), batch.size() * 4);
+    save(".any_single.u8", any_single.data(), any_single.size());
+    save(".any_batch.u8", any_batch.data(), any_batch.size());
+    rtg_grid_info gi = acc->gridInfo();
+    std::printf("{\"res\": [%d, %d, %d], \"nrefs\": %lld}\n", gi.res[0], gi.res[1], gi.res[2], (long long)gi.nrefs);
+    return 0;
+}

@@ -37,7 +37,10 @@ def test_batch_build_equals_scene_builds(gridlib, oracle):
         assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
 
 
-def test_batch_trace_equals_scene_traces(gridlib):
+@pytest.mark.parametrize("cell_records", [False, True])
+def test_batch_trace_equals_scene_traces(gridlib, cell_records):
+    """Also with cell-ordered records written by the batched build (every
+    other scene) and read by the batched trace."""
     import torch
     items = _items()
     scs, tasks, outs = [], [], []
@@ -45,6 +48,8 @@ def test_batch_trace_equals_scene_traces(gridlib):
     for i, it in enumerate(items):
         s = gridlib.Scene(0)
         s.set_geometry(it.scene.verts, it.scene.idx)
+        if cell_records and i % 2 == 0:
+            s.set_tuning(cell_records=True)
         scs.append(s)
         n = it.rays.shape[0]
         if i % 3 == 2:       # any-hit task with tmax 0.5

@@ -161,6 +161,65 @@ def test_results_independent_of_launch_tuning(gridlib, oracle):
                     assert np.array_equal(a, b), (er, persistent)
 
 
+def _frame(s, cam, order="morton8"):
+    import torch
+    n = cam.width * cam.height
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    s.trace_frame_device(cam, scenes.SPHERE_LIGHT, d_hits, d_occ, d_sr, order=order)
+    torch.cuda.synchronize()
+    return d_hits.cpu().numpy(), d_occ.cpu().numpy(), d_sr.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("heavy", [1, 16, 64])
+def test_heavy_cell_deferral_is_exact(gridlib, oracle, heavy):
+    """Rays handed to the warp-per-ray pass (lists longer than `heavy`) get
+    the same hit words, shadow rays and occlusion bits as the one-lane walk,
+    with and without cell-ordered records; heavy=1 on a 1024^2 frame also
+    overflows the per-launch queue, so the in-place fallback runs too."""
+    sc = scenes.deforming_sphere(2)
+    s = _scene(gridlib, sc, 8)
+    cam = scenes.deforming_sphere_camera(1024, 1024) if heavy == 1 else scenes.deforming_sphere_camera(512, 512)
+    s.set_tuning(heavy_cell=0, cell_records=False)
+    ref = _frame(s, cam)
+    for crec in (False, True):
+        s.set_tuning(heavy_cell=heavy, cell_records=crec)
+        s.build(8)
+        out = _frame(s, cam)
+        for a, b in zip(ref, out):
+            assert np.array_equal(a, b), (heavy, crec)
+    # the nearest / any entry points on explicit rays agree as well
+    rng = np.random.default_rng(11)
+    rays = scenes.random_rays(rng, 50_000, (-1.2, -1.2, -1.2), (1.2, 1.2, 1.2))
+    s.set_tuning(heavy_cell=0, cell_records=False)
+    s.build(8)
+    h0 = s.trace_nearest(rays)
+    rays_any = rays.copy()
+    rays_any[:, 7] = 0.5
+    o0 = s.trace_any(rays_any)
+    s.set_tuning(heavy_cell=heavy, cell_records=True)
+    s.build(8)
+    assert np.array_equal(h0.view(np.int32), s.trace_nearest(rays).view(np.int32))
+    assert np.array_equal(o0, s.trace_any(rays_any))
+
+
+def test_heavy_cell_counters_match_oracle(gridlib, oracle):
+    """Deferred rays are counted once (by the warp-per-ray pass)."""
+    sc = scenes.deforming_sphere(0)
+    s = _scene(gridlib, sc, 8)
+    s.set_tuning(heavy_cell=32)
+    g = oracle.Grid(sc.verts, sc.idx, 8)
+    rays = scenes.camera_rays(scenes.deforming_sphere_camera(512, 512), "morton8")
+    s.counters(reset=True)
+    s.trace_nearest(rays, counters=True)
+    c = s.counters(reset=True)
+    _, oc = g.trace_closest(rays, counters=True)
+    assert c["rays"] == rays.shape[0]
+    assert abs(c["cells"] - int(oc[:, 0].sum())) <= 1e-4 * oc[:, 0].sum()
+    assert abs(c["tests"] - int(oc[:, 1].sum())) <= 1e-3 * oc[:, 1].sum()
+
+
 def test_diffuse_secondary_rays(gridlib, oracle):
     """Skewed-density workload: primary camera rays, then one cosine-weighted
     diffuse ray per hit generated on the device; both generations match the
