@@ -546,7 +546,7 @@ def run_batched(args, rank, ws, local, dist):
         ms, _ = time_batch(b, 2)
         return ms
 
-    space = {"k": (2, 4, 8), "order": ("scanline", "morton8"), "empty_run": (4, 8, 16)}
+    space = {"k": (2, 4, 8), "order": ("scanline", "morton8"), "empty_run": (2, 4, 8)}
     best, allres = autotune.search(measure, space=space, reps=1)
     b = batch_for(best["k"], best["order"])
     b.set_tuning(empty_run=best["empty_run"], persistent=True)

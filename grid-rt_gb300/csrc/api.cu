@@ -280,6 +280,11 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
     if (rc == RTG_OK && cudaMalloc(&s->d_ctr, sizeof(TraceCounters)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "ctr");
     if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, 4 * kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
         rc = fail(RTG_NO_MEMORY, "ray counters");
+    if (rc == RTG_OK && s->tune.heavy_cell > 0 &&
+        cudaMalloc(&s->d_defer, sizeof(int32_t) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
+        s->d_defer = nullptr;
+        rc = fail(RTG_NO_MEMORY, "deferred-ray queues");
+    }
     if (rc == RTG_OK) {
         BuildWork w;
         std::memset(&w, 0, sizeof(w));
@@ -944,7 +949,7 @@ rtg_status rtg_batch_rays(rtg_batch b, int64_t* rays) {
 rtg_status rtg_batch_set_tuning(rtg_batch b, int32_t key, int32_t value) {
     if (!b) return fail(RTG_INVALID_PARAM, "batch is NULL");
     if (key == RTG_TUNE_EMPTY_RUN) {
-        if (value != 4 && value != 8 && value != 16) return fail(RTG_INVALID_PARAM, "empty run must be 4, 8 or 16");
+        if (value != 2 && value != 4 && value != 8 && value != 16) return fail(RTG_INVALID_PARAM, "empty run must be 2, 4, 8 or 16");
         b->tune.empty_run = value;
         return RTG_OK;
     }
@@ -972,7 +977,7 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
     if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
     switch (key) {
         case RTG_TUNE_EMPTY_RUN:
-            if (value != 4 && value != 8 && value != 16) return fail(RTG_INVALID_PARAM, "empty run must be 4, 8 or 16");
+            if (value != 2 && value != 4 && value != 8 && value != 16) return fail(RTG_INVALID_PARAM, "empty run must be 2, 4, 8 or 16");
             s->tune.empty_run = value;
             return RTG_OK;
         case RTG_TUNE_PERSISTENT:

@@ -82,10 +82,10 @@ struct TraceCounters {
 
 // Trace launch shape, chosen per scene (rtg_scene_set_tuning / autotuner).
 struct TraceTuning {
-    int empty_run = 8;     // empty cells a lane may walk per loop iteration: 4, 8 or 16
+    int empty_run = 4;     // empty cells a lane may walk per loop iteration: 2, 4, 8 or 16
     int persistent = 1;    // 1: persistent warps over ray batches; 0: one batch per warp
     int cell_records = 0;  // 1: the build also writes triangle records in cell-list order
-    int heavy_cell = 0;    // > 0: rays meeting a list longer than this finish in a warp-per-ray pass
+    int heavy_cell = 32;   // > 0: rays meeting a list longer than this finish in a warp-per-ray pass
 };
 
 // Per-launch device state of a single-scene trace: three counters the launch

@@ -123,7 +123,8 @@ extern "C" rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, co
         return RTG_DEVICE_ERROR;
     }
     TraceTuning tune = scenes[0]->tune;
-    if (opt->empty_run == 4 || opt->empty_run == 8 || opt->empty_run == 16) tune.empty_run = opt->empty_run;
+    if (opt->empty_run == 2 || opt->empty_run == 4 || opt->empty_run == 8 || opt->empty_run == 16)
+        tune.empty_run = opt->empty_run;
 
     // ---- resources (reserved before the clock starts) -----------------------
     unsigned char* d_pool = nullptr;

@@ -464,9 +464,8 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
                     const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
                     if (slot < (unsigned long long)io.defer_cap) {
                         io.defer[slot] = L.ray;
-                        cells = cells0;          // the warp-per-ray pass counts this ray
+                        cells = cells0;          // the warp-per-ray pass counts its cells and tests
                         tests = tests0;
-                        --started;
                         active = false;
                     } else {
                         heavy = kNoHeavy;        // queue full: the lane tests the cell itself
@@ -668,7 +667,8 @@ static void launch_er(const SceneView& s, const TraceIO& io, const TraceTuning& 
 template <int MODE, bool COUNT>
 static void launch_count(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms,
                          cudaStream_t st) {
-    if (tune.empty_run <= 4) launch_er<MODE, COUNT, 4>(s, io, tune, num_sms, st);
+    if (tune.empty_run <= 2) launch_er<MODE, COUNT, 2>(s, io, tune, num_sms, st);
+    else if (tune.empty_run <= 4) launch_er<MODE, COUNT, 4>(s, io, tune, num_sms, st);
     else if (tune.empty_run <= 8) launch_er<MODE, COUNT, 8>(s, io, tune, num_sms, st);
     else launch_er<MODE, COUNT, 16>(s, io, tune, num_sms, st);
 }
@@ -763,7 +763,8 @@ void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* 
     if (total <= 0 || ntasks <= 0) return;
     count_launches(1);
     cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
-    if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
+    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
+    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
     else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
     else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
 }

@@ -23,9 +23,9 @@ CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "tune_c
 
 SPACE = {
     "order": ("scanline", "morton8"),
-    "empty_run": (4, 8, 16),
+    "empty_run": (2, 4, 8),
     "persistent": (True, False),
-    "heavy_cell": (0, 32, 96),
+    "heavy_cell": (0, 12, 24, 48),
     "cell_records": (False, True),
 }
 

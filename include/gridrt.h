@@ -300,13 +300,14 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
                          const rtg_serve_options* opt, rtg_request_times* times);
 
 /* Trace launch shape for this scene (results never depend on it):
- *   RTG_TUNE_EMPTY_RUN   empty cells a ray may walk per loop turn: 4, 8, 16 (default 8)
+ *   RTG_TUNE_EMPTY_RUN   empty cells a ray may walk per loop turn: 2, 4, 8, 16 (default 4)
  *   RTG_TUNE_PERSISTENT  1: persistent warps claim ray batches (default); 0: one batch per warp
  *   RTG_TUNE_CELL_RECORDS 1: builds also store the triangle records in cell-list order
  *                        (48 B per reference) so traces skip the id indirection; from the next build
  *   RTG_TUNE_HEAVY_CELL  n > 0: a ray that meets a cell list longer than n is finished by a
  *                        second pass that traces it with a whole warp (the list split over
- *                        32 lanes); 0 (default) off.  Results are identical either way. */
+ *                        32 lanes); default 32, 0 off.  Results are identical either way.
+ *                        Costs 8 MB of device memory per scene (deferred-ray queues). */
 enum { RTG_TUNE_EMPTY_RUN = 1, RTG_TUNE_PERSISTENT = 2, RTG_TUNE_CELL_RECORDS = 3, RTG_TUNE_HEAVY_CELL = 4 };
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 

@@ -145,7 +145,7 @@ def test_results_independent_of_launch_tuning(gridlib, oracle):
     cam = scenes.deforming_sphere_camera(256, 256)
     n = cam.width * cam.height
     ref = None
-    for er in (4, 8, 16):
+    for er in (2, 4, 8, 16):
         for persistent in (True, False):
             s.set_tuning(empty_run=er, persistent=persistent)
             d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
