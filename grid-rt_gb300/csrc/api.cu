@@ -281,7 +281,7 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
     if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, 4 * kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
         rc = fail(RTG_NO_MEMORY, "ray counters");
     if (rc == RTG_OK && s->tune.heavy_cell > 0 &&
-        cudaMalloc(&s->d_defer, sizeof(int32_t) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
+        cudaMalloc(&s->d_defer, sizeof(int2) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
         s->d_defer = nullptr;
         rc = fail(RTG_NO_MEMORY, "deferred-ray queues");
     }
@@ -768,7 +768,8 @@ struct rtg_batch_s {
     int ntasks = 0;
     long long total = 0;                   // flattened, 32-aligned ray space
     long long rays = 0;
-    unsigned long long* d_counter = nullptr;
+    unsigned long long* d_counter = nullptr;   // ray claims, deferred rays, deferred claims
+    int2* d_defer = nullptr;                   // deferred-ray queue (kDeferCap entries)
     TraceTuning tune;
     int* d_first = nullptr;                // kBuildKinds prefix tables of ntasks + 1 ints
     BatchGrid grid{};
@@ -881,7 +882,8 @@ rtg_status rtg_batch_create(const rtg_scene* scenes, int32_t nscenes, const int3
     if (cudaMalloc(&b->d_build, sizeof(BuildArgs) * nscenes) != cudaSuccess ||
         cudaMalloc(&b->d_scenes, sizeof(BatchScene) * nscenes) != cudaSuccess ||
         cudaMalloc(&b->d_tasks, sizeof(BatchTask) * (ht.size() + 1)) != cudaSuccess ||
-        cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&b->d_counter, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&b->d_defer, sizeof(int2) * kDeferCap) != cudaSuccess ||
         cudaMalloc(&b->d_first, sizeof(int) * kBuildKinds * (nscenes + 1)) != cudaSuccess)
         rc = fail(RTG_NO_MEMORY, "batch tables");
     if (rc == RTG_OK && ht.size() &&
@@ -921,8 +923,8 @@ rtg_status rtg_batch_trace_async(rtg_batch b, void* stream) {
     cudaStream_t st = stream ? (cudaStream_t)stream : b->scenes[0]->stream;
     rtg_status rc = batch_upload_views(b, st, false);
     if (rc) return rc;
-    launch_trace_batch(b->d_scenes, (int)b->scenes.size(), b->d_tasks, b->ntasks, b->total, b->d_counter, b->tune,
-                       b->num_sms, st);
+    launch_trace_batch(b->d_scenes, (int)b->scenes.size(), b->d_tasks, b->ntasks, b->total,
+                       TraceSlot{b->d_counter, b->d_defer, kDeferCap}, b->tune, b->num_sms, st);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;
 }
@@ -957,6 +959,11 @@ rtg_status rtg_batch_set_tuning(rtg_batch b, int32_t key, int32_t value) {
         b->tune.persistent = value ? 1 : 0;
         return RTG_OK;
     }
+    if (key == RTG_TUNE_HEAVY_CELL) {
+        if (value < 0) return fail(RTG_INVALID_PARAM, "heavy-cell threshold must be >= 0");
+        b->tune.heavy_cell = value;
+        return RTG_OK;
+    }
     return fail(RTG_INVALID_PARAM, "unknown tuning key");
 }
 
@@ -968,6 +975,7 @@ rtg_status rtg_batch_destroy(rtg_batch b) {
     cudaFree(b->d_scenes);
     cudaFree(b->d_tasks);
     cudaFree(b->d_counter);
+    cudaFree(b->d_defer);
     cudaFree(b->d_first);
     delete b;
     return RTG_OK;
@@ -987,7 +995,7 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
             if (value < 0) return fail(RTG_INVALID_PARAM, "heavy-cell threshold must be >= 0");
             if (value > 0 && !s->d_defer) {
                 CUDA_TRY(cudaSetDevice(s->device));
-                if (cudaMalloc(&s->d_defer, sizeof(int32_t) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
+                if (cudaMalloc(&s->d_defer, sizeof(int2) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
                     s->d_defer = nullptr;
                     return fail(RTG_NO_MEMORY, "deferred-ray queues");
                 }

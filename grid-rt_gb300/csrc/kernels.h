@@ -93,7 +93,7 @@ struct TraceTuning {
 // queue; launches that may overlap need distinct slots.
 struct TraceSlot {
     unsigned long long* ctr;
-    int32_t* defer;
+    int2* defer;          // {ray, cell} entries
     int32_t defer_cap;
 };
 
@@ -119,7 +119,7 @@ struct BatchTask {
     int32_t mode;          // 0 closest, 1 any
 };
 void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
-                        unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st);
+                        const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st);
 
 void launch_deform(const float* base, const float* normals, float* out, int64_t nverts, float amp, float freq,
                    float phase, cudaStream_t st);

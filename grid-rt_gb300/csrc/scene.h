@@ -29,7 +29,7 @@ struct rtg_scene_s {
     uint32_t* d_occ = nullptr;
     int64_t occ_cap = 0;
     unsigned long long* d_ray_ctr = nullptr;   // ring of per-launch counters, 4 words a slot
-    int32_t* d_defer = nullptr;                // ring of per-launch deferred-ray queues (tune.heavy_cell)
+    int2* d_defer = nullptr;                   // ring of per-launch deferred-ray queues (tune.heavy_cell)
     unsigned ctr_seq = 0;
     gridrt::TraceTuning tune;
     int32_t* d_ids = nullptr;
@@ -59,8 +59,8 @@ struct rtg_scene_s {
 };
 
 namespace gridrt {
-constexpr unsigned kRayCounters = 64;
-constexpr int32_t kDeferCap = 32768;    // deferred rays a launch can queue; more are traced in place
+constexpr unsigned kRayCounters = 32;
+constexpr int32_t kDeferCap = 65536;    // deferred rays a launch can queue; more are traced in place
 // Read-only device view of a built scene (for the trace kernels).
 SceneView scene_view(rtg_scene s);
 // Next per-launch counter slot (and deferred-ray queue) of the scene.

@@ -38,7 +38,8 @@ struct Step {
     cudaEvent_t done = nullptr;
     BatchTask* h_tasks = nullptr;   // pinned
     BatchTask* d_tasks = nullptr;
-    unsigned long long* d_counter = nullptr;
+    unsigned long long* d_counter = nullptr;   // ray claims, deferred rays, deferred claims
+    int2* d_defer = nullptr;                   // deferred-ray queue of the step's launch
     std::vector<int64_t> reqs;
     int64_t pool_end = 0;           // pool head after this step's allocations
     bool busy = false;
@@ -139,6 +140,7 @@ extern "C" rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, co
             if (s.h_tasks) cudaFreeHost(s.h_tasks);
             cudaFree(s.d_tasks);
             cudaFree(s.d_counter);
+            cudaFree(s.d_defer);
         }
         cudaFree(d_pool);
         cudaFree(d_scenes);
@@ -151,7 +153,8 @@ extern "C" rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, co
             cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess ||
             cudaMallocHost(&s.h_tasks, sizeof(BatchTask) * kMaxStepTasks) != cudaSuccess ||
             cudaMalloc(&s.d_tasks, sizeof(BatchTask) * kMaxStepTasks) != cudaSuccess ||
-            cudaMalloc(&s.d_counter, sizeof(unsigned long long)) != cudaSuccess)
+            cudaMalloc(&s.d_counter, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaMalloc(&s.d_defer, sizeof(int2) * kDeferCap) != cudaSuccess)
             rc = RTG_NO_MEMORY;
     }
     if (rc == RTG_OK) {
@@ -249,8 +252,9 @@ extern "C" rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, co
                 } else {
                     cudaMemcpyAsync(s.d_tasks, s.h_tasks, sizeof(BatchTask) * ntasks, cudaMemcpyHostToDevice,
                                     s.stream);
-                    launch_trace_batch(d_scenes, nscenes, s.d_tasks, ntasks, first, s.d_counter, tune,
-                                       scenes[0]->num_sms, s.stream);
+                    launch_trace_batch(d_scenes, nscenes, s.d_tasks, ntasks, first,
+                                       TraceSlot{s.d_counter, s.d_defer, kDeferCap}, tune, scenes[0]->num_sms,
+                                       s.stream);
                 }
                 for (int t = 0; t < ntasks; ++t) {
                     const rtg_request& q = reqs[s.reqs[t]];

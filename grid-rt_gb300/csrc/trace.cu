@@ -189,7 +189,7 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
             const int32_t b = __ldg(offsets + c), e = __ldg(offsets + c + 1);
             if (e - b > heavy) {
                 // long list: the ray goes to the warp-per-ray pass, which
-                // walks it again from the start (this cell is not counted)
+                // resumes the walk at this cell (and counts it)
                 --cells;
                 L.id = kDeferred;
                 return true;
@@ -312,9 +312,10 @@ struct TraceIO {
     long long n;
     unsigned long long* counter;   // [0] ray claims, [1] deferred rays, [2] deferred claims
     TraceCounters* ctr;
-    int32_t* defer;                // deferred ray indices (nullptr: no deferral)
+    int2* defer;                   // deferred rays {ray index, cell it stopped at} (nullptr: no deferral)
     int32_t defer_cap;
     int32_t heavy;                 // lists longer than this are deferred (kNoHeavy: never)
+    int32_t defer_base;            // added to a deferred ray's index (a batch task's first)
 };
 
 // Loads ray `r` into the lane; false when the ray ends at once (misses the
@@ -441,7 +442,6 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
     bool active = ray < io.n;
     L.ray = (int32_t)ray;
     int32_t heavy = io.heavy;
-    const uint32_t cells0 = cells, tests0 = tests;
     if (active) {
         ++started;
         if (!start_ray<MODE>(P, io, L, L.ray)) {
@@ -463,9 +463,8 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
                 if (d) {
                     const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
                     if (slot < (unsigned long long)io.defer_cap) {
-                        io.defer[slot] = L.ray;
-                        cells = cells0;          // the warp-per-ray pass counts its cells and tests
-                        tests = tests0;
+                        // the walk resumes at this cell in the warp-per-ray pass
+                        io.defer[slot] = make_int2(L.ray + io.defer_base, L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
                         active = false;
                     } else {
                         heavy = kNoHeavy;        // queue full: the lane tests the cell itself
@@ -525,6 +524,75 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(Sce
 // one-lane walk's result.  ANY rays are occluded when that minimum is below
 // tmax -- also the one-lane walk's rule, which accepts every new minimum and
 // stops at the first below tmax.
+template <int MODE>
+__device__ __forceinline__ void wide_ray(const SParams& P, const SceneView& s, const TraceIO& io, int32_t ray,
+                                         int32_t cell, uint32_t& cells, uint32_t& tests) {
+    const int lane = threadIdx.x & 31;
+    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
+    Lane L;
+    L.ray = ray;
+    bool done = !start_ray<MODE>(P, io, L, L.ray);
+    if (done && L.id != -2) L.id = -1;
+    if (!done) {
+        // Resume at `cell`: every coordinate moved monotonically from the
+        // start cell, one step per crossing of its axis, each adding tD to
+        // tM -- replaying those additions in order gives the walk's exact
+        // state there (and the earlier cells were tested without a hit).
+        const int32_t z = cell / nxy, y = (cell - z * nxy) / nx, x = cell - z * nxy - y * nx;
+        const int32_t sx = abs(x - L.x), sy = abs(y - L.y), sz = abs(z - L.z);
+        for (int32_t i = 0; i < sx; ++i) L.tMx = fadd(L.tMx, L.tDx);
+        for (int32_t i = 0; i < sy; ++i) L.tMy = fadd(L.tMy, L.tDy);
+        for (int32_t i = 0; i < sz; ++i) L.tMz = fadd(L.tMz, L.tDz);
+        L.x = x;
+        L.y = y;
+        L.z = z;
+        L.budget -= sx + sy + sz;
+    }
+    while (!done) {
+        ++cells;
+        const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+        if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
+            const int32_t c = L.x + L.y * nx + L.z * nxy;
+            const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
+            const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+            tests += (uint32_t)(e - b);
+            for (int32_t i = b + lane; i < e; i += 32) {
+                int32_t tid;
+                float4 A, B, C;
+                if (s.crec) {
+                    A = __ldg(s.crec + 3 * (int64_t)i);
+                    B = __ldg(s.crec + 3 * (int64_t)i + 1);
+                    C = __ldg(s.crec + 3 * (int64_t)i + 2);
+                    tid = __float_as_int(A.w);
+                } else {
+                    tid = __ldg(s.ids + i);
+                    A = __ldg(s.tris + 3 * (int64_t)tid);
+                    B = __ldg(s.tris + 3 * (int64_t)tid + 1);
+                    C = __ldg(s.tris + 3 * (int64_t)tid + 2);
+                }
+                test_tri<MODE_NEAREST>(L, tid, A, B, C, hi);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ot = __shfl_xor_sync(FULL, L.best, o);
+                const int32_t oid = __shfl_xor_sync(FULL, L.id, o);
+                if (ot < L.best || (ot == L.best && (uint32_t)oid < (uint32_t)L.id)) {
+                    L.best = ot;
+                    L.id = oid;
+                }
+            }
+            if (L.best < kFltMax) {
+                if (MODE == MODE_ANY && !(L.best < L.tmax)) L.id = -1;
+                done = true;
+            }
+        }
+        if (!done && dda_step(P, L)) {
+            L.id = -1;
+            done = true;
+        }
+    }
+    if (lane == 0) finish_ray<MODE>(io, P, s.tris, L);
+}
+
 template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io) {
     __shared__ SParams P;
@@ -532,60 +600,14 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
     const int lane = threadIdx.x & 31;
     unsigned long long nd = io.counter[1];
     if (nd > (unsigned long long)io.defer_cap) nd = (unsigned long long)io.defer_cap;
-    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
     uint32_t cells = 0, tests = 0;
     for (;;) {
         unsigned long long j = 0;
         if (lane == 0) j = atomicAdd(io.counter + 2, 1ull);
         j = __shfl_sync(FULL, j, 0);
         if (j >= nd) break;
-        Lane L;
-        L.ray = __ldg(io.defer + j);
-        bool done = !start_ray<MODE>(P, io, L, L.ray);
-        if (done && L.id != -2) L.id = -1;
-        while (!done) {
-            ++cells;
-            const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
-            if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
-                const int32_t c = L.x + L.y * nx + L.z * nxy;
-                const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
-                const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-                tests += (uint32_t)(e - b);
-                for (int32_t i = b + lane; i < e; i += 32) {
-                    int32_t tid;
-                    float4 A, B, C;
-                    if (s.crec) {
-                        A = __ldg(s.crec + 3 * (int64_t)i);
-                        B = __ldg(s.crec + 3 * (int64_t)i + 1);
-                        C = __ldg(s.crec + 3 * (int64_t)i + 2);
-                        tid = __float_as_int(A.w);
-                    } else {
-                        tid = __ldg(s.ids + i);
-                        A = __ldg(s.tris + 3 * (int64_t)tid);
-                        B = __ldg(s.tris + 3 * (int64_t)tid + 1);
-                        C = __ldg(s.tris + 3 * (int64_t)tid + 2);
-                    }
-                    test_tri<MODE_NEAREST>(L, tid, A, B, C, hi);
-                }
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float ot = __shfl_xor_sync(FULL, L.best, o);
-                    const int32_t oid = __shfl_xor_sync(FULL, L.id, o);
-                    if (ot < L.best || (ot == L.best && (uint32_t)oid < (uint32_t)L.id)) {
-                        L.best = ot;
-                        L.id = oid;
-                    }
-                }
-                if (L.best < kFltMax) {
-                    if (MODE == MODE_ANY && !(L.best < L.tmax)) L.id = -1;
-                    done = true;
-                }
-            }
-            if (!done && dda_step(P, L)) {
-                L.id = -1;
-                done = true;
-            }
-        }
-        if (lane == 0) finish_ray<MODE>(io, P, s.tris, L);
+        const int2 d = __ldg(io.defer + j);
+        wide_ray<MODE>(P, s, io, d.x, d.y, cells, tests);
     }
     if (COUNT) {
         if (lane != 0) cells = tests = 0;
@@ -593,13 +615,25 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
     }
 }
 
+// Task t owning flattened ray index f: the last task with first <= f.
+__device__ __forceinline__ int find_task(const BatchTask* __restrict__ tasks, int ntasks, long long f) {
+    int lo = 0, hi = ntasks - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tasks[mid].first <= f) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Many (scene, ray batch) tasks in one persistent launch.  Task t owns the
 // 32-aligned index range [first, first + n) of one flattened ray space, so a
 // 32-ray claim always falls inside one task: scene and mode are warp-uniform.
 template <int ER>
-__global__ void __launch_bounds__(128) trace_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes,
-                                                          const BatchTask* __restrict__ tasks, int ntasks,
-                                                          long long total, unsigned long long* counter) {
+__global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
+    trace_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes, const BatchTask* __restrict__ tasks,
+                       int ntasks, long long total, unsigned long long* counter, int2* defer, int32_t defer_cap,
+                       int32_t heavy) {
     __shared__ SParams P[kMaxBatchScenes];
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
     __syncthreads();
@@ -611,18 +645,16 @@ __global__ void __launch_bounds__(128) trace_batch_kernel(const BatchScene* __re
         if (lane == 0) b = atomicAdd(counter, 32ull);
         b = __shfl_sync(FULL, b, 0);
         if ((long long)b >= total) break;
-        int lo = 0, hi = ntasks - 1;       // last task with first <= b
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (tasks[mid].first <= (long long)b) lo = mid;
-            else hi = mid - 1;
-        }
-        const BatchTask T = tasks[lo];
+        const BatchTask T = tasks[find_task(tasks, ntasks, (long long)b)];
         const SceneView V = scenes[T.scene].view;
         TraceIO io{};
         io.rays = T.rays;
         io.n = T.n;
-        io.heavy = kNoHeavy;
+        io.counter = counter;
+        io.defer = defer;
+        io.defer_cap = defer_cap;
+        io.heavy = defer ? heavy : kNoHeavy;
+        io.defer_base = (int32_t)T.first;
         const long long base = (long long)b - T.first;
         if (T.mode == MODE_ANY) {
             io.occ = static_cast<uint8_t*>(T.out);
@@ -630,6 +662,40 @@ __global__ void __launch_bounds__(128) trace_batch_kernel(const BatchScene* __re
         } else {
             io.hits = static_cast<int4*>(T.out);
             trace_batch32<MODE_NEAREST, ER>(P[T.scene], V, io, L, base, cells, tests, started);
+        }
+    }
+}
+
+// Warp-per-ray pass over the rays a batch launch deferred (flattened indices).
+__global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes,
+                                                               const BatchTask* __restrict__ tasks, int ntasks,
+                                                               unsigned long long* counter,
+                                                               const int2* __restrict__ defer, int32_t defer_cap) {
+    __shared__ SParams P[kMaxBatchScenes];
+    for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    unsigned long long nd = counter[1];
+    if (nd > (unsigned long long)defer_cap) nd = (unsigned long long)defer_cap;
+    uint32_t cells = 0, tests = 0;
+    for (;;) {
+        unsigned long long j = 0;
+        if (lane == 0) j = atomicAdd(counter + 2, 1ull);
+        j = __shfl_sync(FULL, j, 0);
+        if (j >= nd) break;
+        const int2 d = __ldg(defer + j);
+        const long long f = d.x;
+        const BatchTask T = tasks[find_task(tasks, ntasks, f)];
+        const SceneView V = scenes[T.scene].view;
+        TraceIO io{};
+        io.rays = T.rays;
+        io.n = T.n;
+        if (T.mode == MODE_ANY) {
+            io.occ = static_cast<uint8_t*>(T.out);
+            wide_ray<MODE_ANY>(P[T.scene], V, io, (int32_t)(f - T.first), d.y, cells, tests);
+        } else {
+            io.hits = static_cast<int4*>(T.out);
+            wide_ray<MODE_NEAREST>(P[T.scene], V, io, (int32_t)(f - T.first), d.y, cells, tests);
         }
     }
 }
@@ -745,7 +811,7 @@ void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, 
 
 template <int ER>
 static void launch_batch_er(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
-                            unsigned long long* counter, int num_sms, cudaStream_t st) {
+                            const TraceSlot& slot, int32_t heavy, int num_sms, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
@@ -755,18 +821,32 @@ static void launch_batch_er(const BatchScene* scenes, int nscenes, const BatchTa
     long long blocks = (total + 127) / 128;
     blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
     if (blocks < 1) blocks = 1;
-    trace_batch_kernel<ER><<<(int)blocks, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, total, counter);
+    trace_batch_kernel<ER><<<(int)blocks, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, total, slot.ctr,
+                                                         heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy);
 }
 
 void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
-                        unsigned long long* counter, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+                        const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     if (total <= 0 || ntasks <= 0) return;
-    count_launches(1);
-    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
-    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
-    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
-    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
-    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, counter, num_sms, st);
+    // deferred entries are int32 flattened indices
+    const bool defer = tune.heavy_cell > 0 && slot.defer && slot.defer_cap > 0 && total <= 0x7fffffffLL;
+    const int32_t heavy = defer ? tune.heavy_cell : 0;
+    count_launches(defer ? 2 : 1);
+    cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
+    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
+    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
+    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
+    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
+    if (defer) {
+        static int per_sm = 0;
+        if (per_sm == 0) {
+            int b = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_batch_kernel, 128, 0);
+            per_sm = b > 0 ? b : 1;
+        }
+        trace_wide_batch_kernel<<<per_sm * num_sms, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, slot.ctr,
+                                                                  slot.defer, slot.defer_cap);
+    }
 }
 
 void launch_deform(const float* base, const float* normals, float* out, int64_t nverts, float amp, float freq,

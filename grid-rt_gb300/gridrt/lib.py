@@ -367,7 +367,9 @@ class Batch:
         check(load().rtg_batch_rays(self.h, C.byref(r)))
         return r.value
 
-    def set_tuning(self, empty_run: int = None, persistent: bool = None):
+    def set_tuning(self, empty_run: int = None, persistent: bool = None, heavy_cell: int = None):
+        if heavy_cell is not None:
+            check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_HEAVY_CELL, int(heavy_cell)))
         if empty_run is not None:
             check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:

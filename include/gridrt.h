@@ -262,6 +262,8 @@ rtg_status rtg_batch_trace_async(rtg_batch batch, void* stream);
 rtg_status rtg_batch_check(rtg_batch batch, void* stream);
 /* Total rays over the batch's tasks. */
 rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
+/* Keys RTG_TUNE_EMPTY_RUN, RTG_TUNE_PERSISTENT and RTG_TUNE_HEAVY_CELL, as for
+ * rtg_scene_set_tuning; cell-ordered records are a per-scene setting. */
 rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
 rtg_status rtg_batch_destroy(rtg_batch batch);
 
@@ -307,7 +309,7 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *   RTG_TUNE_HEAVY_CELL  n > 0: a ray that meets a cell list longer than n is finished by a
  *                        second pass that traces it with a whole warp (the list split over
  *                        32 lanes); default 32, 0 off.  Results are identical either way.
- *                        Costs 8 MB of device memory per scene (deferred-ray queues). */
+ *                        Costs 16 MB of device memory per scene (deferred-ray queues). */
 enum { RTG_TUNE_EMPTY_RUN = 1, RTG_TUNE_PERSISTENT = 2, RTG_TUNE_CELL_RECORDS = 3, RTG_TUNE_HEAVY_CELL = 4 };
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 

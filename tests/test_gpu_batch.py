@@ -37,10 +37,12 @@ def test_batch_build_equals_scene_builds(gridlib, oracle):
         assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
 
 
-@pytest.mark.parametrize("cell_records", [False, True])
-def test_batch_trace_equals_scene_traces(gridlib, cell_records):
+@pytest.mark.parametrize("cell_records,heavy", [(False, 0), (True, 32), (False, 4)])
+def test_batch_trace_equals_scene_traces(gridlib, cell_records, heavy):
     """Also with cell-ordered records written by the batched build (every
-    other scene) and read by the batched trace."""
+    other scene) and read by the batched trace, and with the batch's
+    warp-per-ray pass (heavy > 0; heavy = 4 also overflows its queue) against
+    per-scene traces without it."""
     import torch
     items = _items()
     scs, tasks, outs = [], [], []
@@ -50,6 +52,7 @@ def test_batch_trace_equals_scene_traces(gridlib, cell_records):
         s.set_geometry(it.scene.verts, it.scene.idx)
         if cell_records and i % 2 == 0:
             s.set_tuning(cell_records=True)
+        s.set_tuning(heavy_cell=0)
         scs.append(s)
         n = it.rays.shape[0]
         if i % 3 == 2:       # any-hit task with tmax 0.5
@@ -63,6 +66,7 @@ def test_batch_trace_equals_scene_traces(gridlib, cell_records):
             tasks.append((i, gridlib.RTG_MODE_NEAREST, d_rays[i], n, out))
         outs.append(out)
     b = gridlib.Batch(scs, [4] * len(items), tasks)
+    b.set_tuning(heavy_cell=heavy)
     b.build_async()
     b.trace_async()
     assert b.check() == 0
