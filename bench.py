@@ -626,6 +626,145 @@ def run_batched(args, rank, ws, local, dist):
 
 
 # ---------------------------------------------------------------------------
+# skewed density: 1,048,576 triangles (90% small in a 0.1^3 box, 10% large in
+# [-4,4]^3); per step a grid build, 1024^2 primary camera rays and one
+# cosine-weighted diffuse secondary ray per primary hit (generated on the
+# device, seeded per step), both traced closest-hit; t / u / v errors of the
+# reported hits against a float64 Moller-Trumbore recomputation
+# ---------------------------------------------------------------------------
+def _fp64_errors(verts, idx, rays, hits):
+    """Max / mean error of the reported t (relative) and u, v (absolute) of
+    every hit against float64 Moller-Trumbore on the same ray and triangle."""
+    ok = hits["id"] >= 0
+    tri = hits["id"][ok]
+    r = rays[ok].astype(np.float64)
+    o, d = r[:, 0:3], r[:, 4:7]
+    v0 = verts[idx[tri, 0]].astype(np.float64)
+    e1 = verts[idx[tri, 1]].astype(np.float64) - v0
+    e2 = verts[idx[tri, 2]].astype(np.float64) - v0
+    p = np.cross(d, e2)
+    inv = 1.0 / (e1 * p).sum(1)
+    tv = o - v0
+    q = np.cross(tv, e1)
+    u = (tv * p).sum(1) * inv
+    v = (d * q).sum(1) * inv
+    t = (e2 * q).sum(1) * inv
+    et = np.abs(hits["t"][ok] - t) / np.maximum(np.abs(t), 1e-30)
+    eu = np.abs(hits["u"][ok] - u)
+    ev = np.abs(hits["v"][ok] - v)
+    out = {"hits": int(ok.sum())}
+    for name, e in (("t_rel", et), ("u_abs", eu), ("v_abs", ev)):
+        out[name] = {"max": float(e.max()) if e.size else 0.0, "mean": float(e.mean()) if e.size else 0.0,
+                     "above_1e-5": int((e > 1e-5).sum())}
+    return out
+
+
+def run_skewed(args, rank, ws, local, dist):
+    import torch
+    from gridrt import autotune, lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc = scenes.skewed_density()
+    cam = scenes.skewed_density_camera(WIDTH, HEIGHT)
+    npix = WIDTH * HEIGHT
+    s = lib.Scene(local)
+    s.set_geometry(sc.verts, sc.idx)
+    stream = torch.cuda.ExternalStream(s.stream, device=dev)
+    d_hits = torch.empty((npix, 4), dtype=torch.int32, device=dev)
+    d_sec = torch.empty((npix, 8), dtype=torch.float32, device=dev)
+    d_hits2 = torch.empty((npix, 4), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for k in LAMBDAS:
+        s.build(k)          # capacities for every k (untimed)
+
+    def step(k, seed, order, ev=None):
+        with torch.cuda.stream(stream):
+            if ev:
+                ev[0].record(stream)
+            s.build_async(k)
+            if ev:
+                ev[1].record(stream)
+            s.trace_camera_diffuse_device(cam, seed, d_hits, d_sec, order=order)
+            s.trace_nearest_device(d_sec, npix, d_hits2)
+            if ev:
+                ev[2].record(stream)
+
+    def measure(cfg):
+        _apply_tuning(s, cfg)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        step(cfg["k"], 1, cfg["order"])
+        step(cfg["k"], 2, cfg["order"], ev)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[2])
+
+    fixed = _parse_tuning(args.fixed_tuning)
+    if fixed:
+        best, allres = dict(fixed), []
+    else:
+        space = {"k": LAMBDAS, "order": ("scanline", "morton8"), "empty_run": (2, 4, 8), "persistent": (True,),
+                 "heavy_cell": (0, 24, 48), "heavy_lanes": (4, 8, 16), "cell_records": (False, True)}
+        best, allres = autotune.search(measure, space=space, reps=2)
+    _apply_tuning(s, best)
+    k, order = best["k"], best["order"]
+    for w in range(args.warmup):
+        step(k, 100 + w, order)
+    torch.cuda.synchronize()
+    if s.build_check() != 0:
+        raise RuntimeError("warm-up build failed: " + lib.load().rtg_last_error().decode())
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    nsec = torch.zeros((), dtype=torch.int64, device=dev)
+    sampler = ClockSampler(local).start() if rank == 0 else None
+    _barrier(dist)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.mark()
+    lc0 = lib.kernel_launches()
+    for st in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()                      # L2 flush between steps (outside the events)
+        step(k, 1000 + st, order, evs[st])
+        with torch.cuda.stream(stream):
+            nsec += (d_sec[:, 7] > 0).sum()    # secondary rays traced (outside the events)
+    lc1 = lib.kernel_launches()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.unmark()
+        sampler.stop()
+    build_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    step_ms = [e[0].elapsed_time(e[2]) for e in evs]
+    t_ms = _max_over_ranks(sum(step_ms), dist)
+    rays = _sum_over_ranks(npix * args.steps + int(nsec.item()), dist)
+
+    # errors of the last step's hits (primary rays regenerated on the host
+    # bit-identically; secondary rays as the device wrote them)
+    prim_rays = scenes.camera_rays(cam, order)
+    prim = lib.split_hits(d_hits.cpu().numpy())
+    sec_rays = d_sec.cpu().numpy()
+    sec = lib.split_hits(d_hits2.cpu().numpy())
+    err = {"primary": _fp64_errors(sc.verts, sc.idx, prim_rays, prim),
+           "secondary": _fp64_errors(sc.verts, sc.idx, sec_rays, sec)}
+    if rank != 0:
+        return
+    clocks = sampler.summary() if sampler else {}
+    print(json.dumps({
+        "metric": "Mrays/s (primary + diffuse secondary, grid build included)",
+        "value": round(rays / t_ms / 1e3, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "skewed_density_1048576tri_1024x1024_diffuse", "k": k, "ray_order": order,
+                   "tuning": best, "triangles": sc.ntris, "rays_per_step": round(rays / args.steps / ws),
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)"},
+        "build_ms": round(statistics.median(build_ms), 4),
+        "fp64_error": err,
+        "gpu_launches": int(lc1 - lc0),
+        "autotune": [(c, round(m, 4)) for c, m in allres],
+        "clocks": {"sm_mhz": clocks.get("sm_mhz"), "sm_max_mhz": clocks.get("sm_max_mhz"),
+                   "reasons": clocks.get("reasons", []), "samples": clocks.get("samples", 0)},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # serving: 16 resident scenes, Poisson request streams, continuous batching
 # (rtg_serve_run) versus the plain one-request-at-a-time path
 # ---------------------------------------------------------------------------
@@ -722,13 +861,14 @@ def _parse_tuning(text):
     yes = lambda v: v not in ("0", "false", "False")
     return {"k": int(d.get("k", 8)), "order": d.get("order", "morton8"), "empty_run": int(d.get("empty_run", 4)),
             "persistent": yes(d.get("persistent", "0")), "heavy_cell": int(d.get("heavy_cell", 0)),
-            "cell_records": yes(d.get("cell_records", "0"))}
+            "heavy_lanes": int(d.get("heavy_lanes", 8)), "cell_records": yes(d.get("cell_records", "0"))}
 
 
 def _apply_tuning(scene, cfg):
     """Launch-shape settings of one candidate; cell records take effect at the next build."""
     scene.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"],
-                     heavy_cell=cfg.get("heavy_cell", 0), cell_records=cfg.get("cell_records", False))
+                     heavy_cell=cfg.get("heavy_cell", 0), heavy_lanes=cfg.get("heavy_lanes", 8),
+                     cell_records=cfg.get("cell_records", False))
 
 
 def main():
@@ -737,7 +877,7 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
-    ap.add_argument("--workload", default="deforming", choices=["deforming", "batched", "serving"])
+    ap.add_argument("--workload", default="deforming", choices=["deforming", "batched", "serving", "skewed"])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
     ap.add_argument("--fixed-tuning", default="",
@@ -751,6 +891,8 @@ def main():
         run_batched(args, rank, ws, local, dist)
     elif args.workload == "serving":
         run_serving(args, rank, ws, local, dist)
+    elif args.workload == "skewed":
+        run_skewed(args, rank, ws, local, dist)
     else:
         run_gpu(args, rank, ws, local, dist)
     if dist is not None:

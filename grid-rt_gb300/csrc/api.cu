@@ -76,7 +76,7 @@ rtg_status ensure_grid_buffers(rtg_scene s, int64_t cells_plus_one, int64_t refs
     const int64_t R = ref_capacity(s);
     CUDA_TRY(grow(s->d_qs, s->qs_cap, R / 2 + 2));
     CUDA_TRY(grow(s->d_qm, s->qm_cap, R / 33 + 2));
-    CUDA_TRY(grow(s->d_ql, s->ql_cap, R / 4097 + 2));
+    CUDA_TRY(grow(s->d_ql, s->ql_cap, R / (SORT_MED_MAX + 1) + 2));
     return RTG_OK;
 }
 
@@ -964,6 +964,12 @@ rtg_status rtg_batch_set_tuning(rtg_batch b, int32_t key, int32_t value) {
         b->tune.heavy_cell = value;
         return RTG_OK;
     }
+    if (key == RTG_TUNE_HEAVY_LANES) {
+        if (value != 4 && value != 8 && value != 16 && value != 32)
+            return fail(RTG_INVALID_PARAM, "heavy lanes must be 4, 8, 16 or 32");
+        b->tune.heavy_lanes = value;
+        return RTG_OK;
+    }
     return fail(RTG_INVALID_PARAM, "unknown tuning key");
 }
 
@@ -1001,6 +1007,11 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
                 }
             }
             s->tune.heavy_cell = value;
+            return RTG_OK;
+        case RTG_TUNE_HEAVY_LANES:
+            if (value != 4 && value != 8 && value != 16 && value != 32)
+                return fail(RTG_INVALID_PARAM, "heavy lanes must be 4, 8, 16 or 32");
+            s->tune.heavy_lanes = value;
             return RTG_OK;
         case RTG_TUNE_CELL_RECORDS:
             // takes effect at the next build (which then also writes the records)

@@ -605,6 +605,30 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             }
             if (mask) atomicOr(&occ[word], mask);
         }
+        // cells to sort, by size class: three 10-bit counts packed in one
+        // word (at most 16 per thread, 512 per warp), one warp scan, one
+        // atomicAdd per warp and class
+        uint32_t packed = 0u;
+#pragma unroll
+        for (int i = 0; i < SCAN_ITEMS; ++i) {
+            const int32_t n = v[i];
+            if (b + i < C && n >= 2) packed += n <= SORT_SMALL_MAX ? 1u : (n <= SORT_MED_MAX ? (1u << 10) : (1u << 20));
+        }
+        uint32_t incl = packed;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        uint32_t base_s = 0u, base_m = 0u, base_l = 0u;
+        if (lane == 31) {
+            if (incl & 1023u) base_s = atomicAdd(&w->nsort[0], incl & 1023u);
+            if ((incl >> 10) & 1023u) base_m = atomicAdd(&w->nsort[1], (incl >> 10) & 1023u);
+            if (incl >> 20) base_l = atomicAdd(&w->nsort[2], incl >> 20);
+        }
+        const uint32_t excl = incl - packed;
+        uint32_t js = __shfl_sync(FULL, base_s, 31) + (excl & 1023u);
+        uint32_t jm = __shfl_sync(FULL, base_m, 31) + ((excl >> 10) & 1023u);
+        uint32_t jl = __shfl_sync(FULL, base_l, 31) + (excl >> 20);
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             if (b + i < C) {
@@ -612,18 +636,18 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
                 counts[b + i] = (int32_t)run;
                 const int32_t n = v[i];
                 if (n >= 2) {
-                    if (n <= 32) {
-                        const uint32_t slot = atomicAdd(&w->nsort[0], 1u);
-                        if (slot < q_small_cap) q_small[slot] = (int32_t)(b + i);
+                    if (n <= SORT_SMALL_MAX) {
+                        if (js < q_small_cap) q_small[js] = (int32_t)(b + i);
                         else raise_status(p, w, ST_SORT_CAP);
-                    } else if (n <= 4096) {
-                        const uint32_t slot = atomicAdd(&w->nsort[1], 1u);
-                        if (slot < q_med_cap) q_med[slot] = (int32_t)(b + i);
+                        ++js;
+                    } else if (n <= SORT_MED_MAX) {
+                        if (jm < q_med_cap) q_med[jm] = (int32_t)(b + i);
                         else raise_status(p, w, ST_SORT_CAP);
+                        ++jm;
                     } else {
-                        const uint32_t slot = atomicAdd(&w->nsort[2], 1u);
-                        if (slot < q_large_cap) q_large[slot] = (int32_t)(b + i);
+                        if (jl < q_large_cap) q_large[jl] = (int32_t)(b + i);
                         else raise_status(p, w, ST_SORT_CAP);
+                        ++jl;
                     }
                 }
             }
@@ -690,36 +714,42 @@ __global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const Bu
     }
 }
 
-static constexpr int MED_MAX = 4096;
+// Cells of 33..256 entries: one warp per cell, bitonic network over a
+// power-of-two pad (64..256) in the warp's own shared-memory slice.
+static constexpr int MED_WARPS = 16;    // warps of a 512-thread block
 
 __device__ __forceinline__ void sort_medium_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, const int32_t* __restrict__ q,
                                                           const BuildWork* w, const GridParams* p, unsigned vbx, unsigned vgx) {
     if (sort_skip(p)) return;
-    __shared__ int32_t a[MED_MAX];
+    __shared__ int32_t sh[MED_WARPS][SORT_MED_MAX];
+    const int lane = threadIdx.x & 31;
+    int32_t* a = sh[threadIdx.x >> 5];
     const uint32_t nq = w->nsort[1];
-    for (int64_t i = vbx; i < nq; i += vgx) {
+    const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
+    for (int64_t i = warp; i < nq; i += nwarps) {
         const int32_t c = q[i];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
         int m = 64;
         while (m < n) m <<= 1;
-        for (int t = threadIdx.x; t < m; t += blockDim.x) a[t] = t < n ? ids[s + t] : INT_MAX;
-        __syncthreads();
+        for (int t = lane; t < m; t += 32) a[t] = t < n ? ids[s + t] : INT_MAX;
+        __syncwarp();
         for (int k = 2; k <= m; k <<= 1) {
             for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int t = threadIdx.x; t < m; t += blockDim.x) {
-                    const int o = t ^ j;
-                    if (o > t) {
-                        const bool up = (t & k) == 0;
-                        const int32_t x = a[t], y = a[o];
-                        if ((x > y) == up) { a[t] = y; a[o] = x; }
-                    }
+                // m/2 compare-exchange pairs: pair r joins t (bit j clear) and t + j
+                for (int r = lane; r < (m >> 1); r += 32) {
+                    const int t = ((r & ~(j - 1)) << 1) | (r & (j - 1));
+                    const int o = t + j;
+                    const bool up = (t & k) == 0;
+                    const int32_t x = a[t], y = a[o];
+                    if ((x > y) == up) { a[t] = y; a[o] = x; }
                 }
-                __syncthreads();
+                __syncwarp();
             }
         }
-        for (int t = threadIdx.x; t < n; t += blockDim.x) ids[s + t] = a[t];
-        __syncthreads();
+        for (int t = lane; t < n; t += 32) ids[s + t] = a[t];
+        __syncwarp();
     }
 }
 
@@ -736,8 +766,10 @@ __global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const B
     }
 }
 
-// Cells above 4096 entries: copy the list to scratch, then per id chunk set
-// one shared-memory bit per id and write the set bits back in order.
+// Cells above 256 entries, one block per cell: up to 4096 entries (and the
+// dynamic shared memory's size) a bitonic network in shared memory; above,
+// copy the list to scratch, then per id chunk set one shared-memory bit per
+// id and write the set bits back in order.
 __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, int32_t* __restrict__ scratch,
                                                           const int32_t* __restrict__ q, const BuildWork* w,
@@ -749,9 +781,32 @@ __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offs
     __shared__ int32_t base_sh;
     const uint32_t nq = w->nsort[2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int bitonic_max = bitmap_words < SORT_BLOCK_MAX ? bitmap_words : SORT_BLOCK_MAX;
     for (int64_t qi = vbx; qi < nq; qi += vgx) {
         const int32_t c = q[qi];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
+        if (n <= bitonic_max) {
+            int32_t* a = reinterpret_cast<int32_t*>(bm);
+            int m = 512;
+            while (m < n) m <<= 1;
+            for (int t = threadIdx.x; t < m; t += blockDim.x) a[t] = t < n ? ids[s + t] : INT_MAX;
+            __syncthreads();
+            for (int k = 2; k <= m; k <<= 1) {
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int r = threadIdx.x; r < (m >> 1); r += blockDim.x) {
+                        const int t = ((r & ~(j - 1)) << 1) | (r & (j - 1));
+                        const int o = t + j;
+                        const bool up = (t & k) == 0;
+                        const int32_t x = a[t], y = a[o];
+                        if ((x > y) == up) { a[t] = y; a[o] = x; }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (int t = threadIdx.x; t < n; t += blockDim.x) ids[s + t] = a[t];
+            __syncthreads();
+            continue;
+        }
         int32_t mn = INT_MAX, mx = INT_MIN;
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int32_t v = ids[s + t];
@@ -870,8 +925,8 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     out[BK_TILE] = clampi((a.cell_cap + SCAN_TILE - 1) / SCAN_TILE, 8 * sms);
     out[BK_ONE] = 1;
     out[BK_SSMALL] = clampi(a.cell_cap / 512 + 1, 8 * sms);
-    out[BK_SMED] = clampi(a.cell_cap / 8192 + 1, 2 * sms);
-    out[BK_SLARGE] = clampi(a.cell_cap / 65536 + 1, sms);
+    out[BK_SMED] = clampi(a.cell_cap / 2048 + 1, 4 * sms);             // 16 warps a block, one cell a warp
+    out[BK_SLARGE] = clampi(a.cell_cap / 16384 + 1, 2 * sms);
     out[BK_REFS] = a.crec ? clampi((a.ref_cap + 255) / 256, 16 * sms) : 0;
 }
 

@@ -40,6 +40,13 @@ enum : uint32_t {
     ST_SORT_CAP = 32u,    // segmented-sort work lists overflowed
 };
 
+// Per-cell sort size classes: warp registers up to 32 entries, one warp's
+// shared-memory slice up to 256, a block above (bitonic up to 4096, bitmap
+// beyond).
+static constexpr int SORT_SMALL_MAX = 32;
+static constexpr int SORT_MED_MAX = 256;
+static constexpr int SORT_BLOCK_MAX = 4096;
+
 // Work state shared by the build kernels of one scene (device memory).
 struct BuildWork {
     uint32_t keys[6];        // ordered-int min xyz, max xyz

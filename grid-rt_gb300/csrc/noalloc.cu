@@ -48,7 +48,7 @@ constexpr size_t kQSmall = kMaxRefs / 2 + 2;
 constexpr size_t kOffQMed = kOffQSmall + ((kQSmall * 4 + 255) / 256) * 256;
 constexpr size_t kQMed = kMaxRefs / 33 + 2;
 constexpr size_t kOffQLarge = kOffQMed + ((kQMed * 4 + 255) / 256) * 256;
-constexpr size_t kQLarge = kMaxRefs / 4097 + 2;
+constexpr size_t kQLarge = kMaxRefs / (SORT_MED_MAX + 1) + 2;
 constexpr size_t kOffScratch = kOffQLarge + ((kQLarge * 4 + 255) / 256) * 256;
 constexpr size_t kArenaBytes = kOffScratch + kMaxRefs * 4;
 

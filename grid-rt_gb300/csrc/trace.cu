@@ -516,47 +516,59 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(Sce
     if (COUNT) flush_counters(io.ctr, started, cells, tests);
 }
 
-// Warp-per-ray pass over the deferred rays: all 32 lanes hold the same ray
-// and walk the same cells; a cell's list is split over the lanes (lane j
-// tests entries j, j+32, ...), each lane keeping the first minimum of its
-// share, and the warp takes the minimum t, ties to the smaller triangle id.
-// Lists are sorted by id, so that is the first minimum in list order: the
-// one-lane walk's result.  ANY rays are occluded when that minimum is below
-// tmax -- also the one-lane walk's rule, which accepts every new minimum and
-// stops at the first below tmax.
-template <int MODE>
-__device__ __forceinline__ void wide_ray(const SParams& P, const SceneView& s, const TraceIO& io, int32_t ray,
-                                         int32_t cell, uint32_t& cells, uint32_t& tests) {
-    const int lane = threadIdx.x & 31;
+// Warp-per-ray pass over the deferred rays, G lanes per ray (32/G rays a
+// warp): the G lanes of a group hold the same ray and walk the same cells; a
+// cell's list is split over them (lane j of the group tests entries j, j+G,
+// ...), each lane keeping the first minimum of its share, and the group
+// takes the minimum t, ties to the smaller triangle id.  Lists are sorted by
+// id, so that is the first minimum in list order: the one-lane walk's result.
+// ANY rays are occluded when that minimum is below tmax -- also the one-lane
+// walk's rule, which accepts every new minimum and stops at the first below
+// tmax.
+//
+// A deferred ray resumes at the cell where its lane stopped: every coordinate
+// moved monotonically from the start cell, one step per crossing of its
+// axis, each adding tD to tM, so replaying those additions in order rebuilds
+// the walk's exact state there (the earlier cells were tested without a hit).
+__device__ __forceinline__ void resume_at(const SParams& P, Lane& L, int32_t cell) {
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
-    Lane L;
-    L.ray = ray;
-    bool done = !start_ray<MODE>(P, io, L, L.ray);
-    if (done && L.id != -2) L.id = -1;
-    if (!done) {
-        // Resume at `cell`: every coordinate moved monotonically from the
-        // start cell, one step per crossing of its axis, each adding tD to
-        // tM -- replaying those additions in order gives the walk's exact
-        // state there (and the earlier cells were tested without a hit).
-        const int32_t z = cell / nxy, y = (cell - z * nxy) / nx, x = cell - z * nxy - y * nx;
-        const int32_t sx = abs(x - L.x), sy = abs(y - L.y), sz = abs(z - L.z);
-        for (int32_t i = 0; i < sx; ++i) L.tMx = fadd(L.tMx, L.tDx);
-        for (int32_t i = 0; i < sy; ++i) L.tMy = fadd(L.tMy, L.tDy);
-        for (int32_t i = 0; i < sz; ++i) L.tMz = fadd(L.tMz, L.tDz);
-        L.x = x;
-        L.y = y;
-        L.z = z;
-        L.budget -= sx + sy + sz;
-    }
-    while (!done) {
-        ++cells;
-        const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
-        if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
-            const int32_t c = L.x + L.y * nx + L.z * nxy;
-            const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
-            const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-            tests += (uint32_t)(e - b);
-            for (int32_t i = b + lane; i < e; i += 32) {
+    const int32_t z = cell / nxy, y = (cell - z * nxy) / nx, x = cell - z * nxy - y * nx;
+    const int32_t sx = abs(x - L.x), sy = abs(y - L.y), sz = abs(z - L.z);
+    for (int32_t i = 0; i < sx; ++i) L.tMx = fadd(L.tMx, L.tDx);
+    for (int32_t i = 0; i < sy; ++i) L.tMy = fadd(L.tMy, L.tDy);
+    for (int32_t i = 0; i < sz; ++i) L.tMz = fadd(L.tMz, L.tDz);
+    L.x = x;
+    L.y = y;
+    L.z = z;
+    L.budget -= sx + sy + sz;
+}
+
+// Walks the group's ray (state in L, identical on its G lanes) to its end.
+// Every lane of the warp calls it; groups that are done idle through the
+// warp-wide list loop and reductions.
+template <int G>
+__device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
+                                          uint32_t& cells, uint32_t& tests) {
+    const int gl = threadIdx.x & (G - 1);
+    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
+    while (__any_sync(FULL, !done)) {
+        int32_t b = 0, e = 0;
+        float hi = 0.0f;
+        if (!done) {
+            if (gl == 0) ++cells;
+            const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+            if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
+                const int32_t c = L.x + L.y * nx + L.z * nxy;
+                b = __ldg(s.offsets + c);
+                e = __ldg(s.offsets + c + 1);
+                hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+                if (gl == 0) tests += (uint32_t)(e - b);
+            }
+        }
+        const unsigned trips = __reduce_max_sync(FULL, (unsigned)((e - b + G - 1) / G));
+        for (unsigned it = 0; it < trips; ++it) {
+            const int32_t i = b + gl + (int32_t)it * G;
+            if (i < e) {
                 int32_t tid;
                 float4 A, B, C;
                 if (s.crec) {
@@ -572,45 +584,62 @@ __device__ __forceinline__ void wide_ray(const SParams& P, const SceneView& s, c
                 }
                 test_tri<MODE_NEAREST>(L, tid, A, B, C, hi);
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ot = __shfl_xor_sync(FULL, L.best, o);
-                const int32_t oid = __shfl_xor_sync(FULL, L.id, o);
-                if (ot < L.best || (ot == L.best && (uint32_t)oid < (uint32_t)L.id)) {
-                    L.best = ot;
-                    L.id = oid;
-                }
+        }
+#pragma unroll
+        for (int o = G >> 1; o > 0; o >>= 1) {
+            const float ot = __shfl_xor_sync(FULL, L.best, o);
+            const int32_t oid = __shfl_xor_sync(FULL, L.id, o);
+            if (ot < L.best || (ot == L.best && (uint32_t)oid < (uint32_t)L.id)) {
+                L.best = ot;
+                L.id = oid;
             }
+        }
+        if (!done) {
             if (L.best < kFltMax) {
-                if (MODE == MODE_ANY && !(L.best < L.tmax)) L.id = -1;
+                if (any && !(L.best < L.tmax)) L.id = -1;
+                done = true;
+            } else if (dda_step(P, L)) {
+                L.id = -1;
                 done = true;
             }
         }
-        if (!done && dda_step(P, L)) {
-            L.id = -1;
-            done = true;
-        }
     }
-    if (lane == 0) finish_ray<MODE>(io, P, s.tris, L);
 }
 
-template <int MODE, bool COUNT>
+template <int MODE, bool COUNT, int G>
 __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io) {
     __shared__ SParams P;
     load_sparams(s.params, P);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), grp = lane / G;
     unsigned long long nd = io.counter[1];
     if (nd > (unsigned long long)io.defer_cap) nd = (unsigned long long)io.defer_cap;
     uint32_t cells = 0, tests = 0;
     for (;;) {
-        unsigned long long j = 0;
-        if (lane == 0) j = atomicAdd(io.counter + 2, 1ull);
-        j = __shfl_sync(FULL, j, 0);
-        if (j >= nd) break;
-        const int2 d = __ldg(io.defer + j);
-        wide_ray<MODE>(P, s, io, d.x, d.y, cells, tests);
+        unsigned long long j0 = 0;
+        if (lane == 0) j0 = atomicAdd(io.counter + 2, (unsigned long long)(32 / G));
+        j0 = __shfl_sync(FULL, j0, 0);
+        if (j0 >= nd) break;
+        const unsigned long long j = j0 + grp;
+        const bool valid = j < nd;
+        bool done = true;
+        Lane L;
+        L.best = kFltMax;
+        L.id = -1;
+        if (valid) {
+            const int2 d = __ldg(io.defer + j);
+            L.ray = d.x;
+            done = !start_ray<MODE>(P, io, L, L.ray);
+            if (done) {
+                if (L.id != -2) L.id = -1;
+            } else {
+                resume_at(P, L, d.y);
+            }
+        }
+        wide_walk<G>(P, s, L, done, MODE == MODE_ANY, cells, tests);
+        if (valid && gl == 0) finish_ray<MODE>(io, P, s.tris, L);
     }
     if (COUNT) {
-        if (lane != 0) cells = tests = 0;
+        if (gl != 0) cells = tests = 0;
         flush_counters(io.ctr, 0, cells, tests);
     }
 }
@@ -666,7 +695,9 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
     }
 }
 
-// Warp-per-ray pass over the rays a batch launch deferred (flattened indices).
+// Warp-per-ray pass over the rays a batch launch deferred (flattened
+// indices); each group resolves its own task, scene and mode.
+template <int G>
 __global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes,
                                                                const BatchTask* __restrict__ tasks, int ntasks,
                                                                unsigned long long* counter,
@@ -674,28 +705,49 @@ __global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene*
     __shared__ SParams P[kMaxBatchScenes];
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, gl = lane & (G - 1), grp = lane / G;
     unsigned long long nd = counter[1];
     if (nd > (unsigned long long)defer_cap) nd = (unsigned long long)defer_cap;
     uint32_t cells = 0, tests = 0;
     for (;;) {
-        unsigned long long j = 0;
-        if (lane == 0) j = atomicAdd(counter + 2, 1ull);
-        j = __shfl_sync(FULL, j, 0);
-        if (j >= nd) break;
-        const int2 d = __ldg(defer + j);
-        const long long f = d.x;
-        const BatchTask T = tasks[find_task(tasks, ntasks, f)];
-        const SceneView V = scenes[T.scene].view;
+        unsigned long long j0 = 0;
+        if (lane == 0) j0 = atomicAdd(counter + 2, (unsigned long long)(32 / G));
+        j0 = __shfl_sync(FULL, j0, 0);
+        if (j0 >= nd) break;
+        const unsigned long long j = j0 + grp;
+        const bool valid = j < nd;
+        bool done = true, any = false;
+        int scene = 0;
+        Lane L;
+        L.best = kFltMax;
+        L.id = -1;
         TraceIO io{};
-        io.rays = T.rays;
-        io.n = T.n;
-        if (T.mode == MODE_ANY) {
-            io.occ = static_cast<uint8_t*>(T.out);
-            wide_ray<MODE_ANY>(P[T.scene], V, io, (int32_t)(f - T.first), d.y, cells, tests);
-        } else {
-            io.hits = static_cast<int4*>(T.out);
-            wide_ray<MODE_NEAREST>(P[T.scene], V, io, (int32_t)(f - T.first), d.y, cells, tests);
+        if (valid) {
+            const int2 d = __ldg(defer + j);
+            const BatchTask T = tasks[find_task(tasks, ntasks, (long long)d.x)];
+            scene = T.scene;
+            any = T.mode == MODE_ANY;
+            io.rays = T.rays;
+            io.n = T.n;
+            L.ray = (int32_t)((long long)d.x - T.first);
+            if (any) {
+                io.occ = static_cast<uint8_t*>(T.out);
+                done = !start_ray<MODE_ANY>(P[scene], io, L, L.ray);
+            } else {
+                io.hits = static_cast<int4*>(T.out);
+                done = !start_ray<MODE_NEAREST>(P[scene], io, L, L.ray);
+            }
+            if (done) {
+                if (L.id != -2) L.id = -1;
+            } else {
+                resume_at(P[scene], L, d.y);
+            }
+        }
+        const SceneView V = scenes[scene].view;
+        wide_walk<G>(P[scene], V, L, done, any, cells, tests);
+        if (valid && gl == 0) {
+            if (any) finish_ray<MODE_ANY>(io, P[scene], V.tris, L);
+            else finish_ray<MODE_NEAREST>(io, P[scene], V.tris, L);
         }
     }
 }
@@ -739,15 +791,24 @@ static void launch_count(const SceneView& s, const TraceIO& io, const TraceTunin
     else launch_er<MODE, COUNT, 16>(s, io, tune, num_sms, st);
 }
 
-template <int MODE, bool COUNT>
-static void launch_wide(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
+template <int MODE, bool COUNT, int G>
+static void launch_wide_g(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_kernel<MODE, COUNT>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_kernel<MODE, COUNT, G>, 128, 0);
         per_sm = b > 0 ? b : 1;
     }
-    trace_wide_kernel<MODE, COUNT><<<per_sm * num_sms, 128, 0, st>>>(s, io);
+    trace_wide_kernel<MODE, COUNT, G><<<per_sm * num_sms, 128, 0, st>>>(s, io);
+}
+
+template <int MODE, bool COUNT>
+static void launch_wide(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms,
+                        cudaStream_t st) {
+    if (tune.heavy_lanes <= 4) launch_wide_g<MODE, COUNT, 4>(s, io, num_sms, st);
+    else if (tune.heavy_lanes <= 8) launch_wide_g<MODE, COUNT, 8>(s, io, num_sms, st);
+    else if (tune.heavy_lanes <= 16) launch_wide_g<MODE, COUNT, 16>(s, io, num_sms, st);
+    else launch_wide_g<MODE, COUNT, 32>(s, io, num_sms, st);
 }
 
 template <int MODE>
@@ -763,8 +824,8 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {
-        if (io.ctr) launch_wide<MODE, true>(s, io, num_sms, st);
-        else launch_wide<MODE, false>(s, io, num_sms, st);
+        if (io.ctr) launch_wide<MODE, true>(s, io, tune, num_sms, st);
+        else launch_wide<MODE, false>(s, io, tune, num_sms, st);
     }
 }
 
@@ -825,6 +886,19 @@ static void launch_batch_er(const BatchScene* scenes, int nscenes, const BatchTa
                                                          heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy);
 }
 
+template <int G>
+static void launch_wide_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks,
+                              const TraceSlot& slot, int num_sms, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_batch_kernel<G>, 128, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    trace_wide_batch_kernel<G><<<per_sm * num_sms, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, slot.ctr,
+                                                                  slot.defer, slot.defer_cap);
+}
+
 void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
                         const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     if (total <= 0 || ntasks <= 0) return;
@@ -838,14 +912,10 @@ void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* 
     else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
     else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
     if (defer) {
-        static int per_sm = 0;
-        if (per_sm == 0) {
-            int b = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_batch_kernel, 128, 0);
-            per_sm = b > 0 ? b : 1;
-        }
-        trace_wide_batch_kernel<<<per_sm * num_sms, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, slot.ctr,
-                                                                  slot.defer, slot.defer_cap);
+        if (tune.heavy_lanes <= 4) launch_wide_batch<4>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);
+        else if (tune.heavy_lanes <= 8) launch_wide_batch<8>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);
+        else if (tune.heavy_lanes <= 16) launch_wide_batch<16>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);
+        else launch_wide_batch<32>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);
     }
 }
 

@@ -26,6 +26,7 @@ RTG_TUNE_EMPTY_RUN = 1
 RTG_TUNE_PERSISTENT = 2
 RTG_TUNE_CELL_RECORDS = 3
 RTG_TUNE_HEAVY_CELL = 4
+RTG_TUNE_HEAVY_LANES = 5
 ORDER = {"scanline": 0, "morton8": 1}
 
 
@@ -315,7 +316,7 @@ class Scene:
                                      stream))
 
     def set_tuning(self, empty_run: int = None, persistent: bool = None, cell_records: bool = None,
-                   heavy_cell: int = None):
+                   heavy_cell: int = None, heavy_lanes: int = None):
         if empty_run is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:
@@ -324,6 +325,8 @@ class Scene:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_CELL_RECORDS, 1 if cell_records else 0))
         if heavy_cell is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_HEAVY_CELL, int(heavy_cell)))
+        if heavy_lanes is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_HEAVY_LANES, int(heavy_lanes)))
 
     def counters(self, reset: bool = True):
         out = (C.c_int64 * 3)()
@@ -367,9 +370,12 @@ class Batch:
         check(load().rtg_batch_rays(self.h, C.byref(r)))
         return r.value
 
-    def set_tuning(self, empty_run: int = None, persistent: bool = None, heavy_cell: int = None):
+    def set_tuning(self, empty_run: int = None, persistent: bool = None, heavy_cell: int = None,
+                   heavy_lanes: int = None):
         if heavy_cell is not None:
             check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_HEAVY_CELL, int(heavy_cell)))
+        if heavy_lanes is not None:
+            check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_HEAVY_LANES, int(heavy_lanes)))
         if empty_run is not None:
             check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:

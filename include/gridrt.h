@@ -262,8 +262,9 @@ rtg_status rtg_batch_trace_async(rtg_batch batch, void* stream);
 rtg_status rtg_batch_check(rtg_batch batch, void* stream);
 /* Total rays over the batch's tasks. */
 rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
-/* Keys RTG_TUNE_EMPTY_RUN, RTG_TUNE_PERSISTENT and RTG_TUNE_HEAVY_CELL, as for
- * rtg_scene_set_tuning; cell-ordered records are a per-scene setting. */
+/* Keys RTG_TUNE_EMPTY_RUN, RTG_TUNE_PERSISTENT, RTG_TUNE_HEAVY_CELL and
+ * RTG_TUNE_HEAVY_LANES, as for rtg_scene_set_tuning; cell-ordered records are
+ * a per-scene setting. */
 rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
 rtg_status rtg_batch_destroy(rtg_batch batch);
 
@@ -307,10 +308,17 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *   RTG_TUNE_CELL_RECORDS 1: builds also store the triangle records in cell-list order
  *                        (48 B per reference) so traces skip the id indirection; from the next build
  *   RTG_TUNE_HEAVY_CELL  n > 0: a ray that meets a cell list longer than n is finished by a
- *                        second pass that traces it with a whole warp (the list split over
- *                        32 lanes); default 32, 0 off.  Results are identical either way.
- *                        Costs 16 MB of device memory per scene (deferred-ray queues). */
-enum { RTG_TUNE_EMPTY_RUN = 1, RTG_TUNE_PERSISTENT = 2, RTG_TUNE_CELL_RECORDS = 3, RTG_TUNE_HEAVY_CELL = 4 };
+ *                        second pass that traces it with a group of lanes (the list split
+ *                        over them); default 32, 0 off.  Results are identical either way.
+ *                        Costs 16 MB of device memory per scene (deferred-ray queues).
+ *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8 (default), 16, 32 */
+enum {
+    RTG_TUNE_EMPTY_RUN = 1,
+    RTG_TUNE_PERSISTENT = 2,
+    RTG_TUNE_CELL_RECORDS = 3,
+    RTG_TUNE_HEAVY_CELL = 4,
+    RTG_TUNE_HEAVY_LANES = 5
+};
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 
 /* Counters accumulated by calls made with RTG_TRACE_COUNTERS since the last

@@ -66,7 +66,7 @@ def test_batch_trace_equals_scene_traces(gridlib, cell_records, heavy):
             tasks.append((i, gridlib.RTG_MODE_NEAREST, d_rays[i], n, out))
         outs.append(out)
     b = gridlib.Batch(scs, [4] * len(items), tasks)
-    b.set_tuning(heavy_cell=heavy)
+    b.set_tuning(heavy_cell=heavy, heavy_lanes=4 if heavy == 4 else 8)
     b.build_async()
     b.trace_async()
     assert b.check() == 0

@@ -44,14 +44,22 @@ def test_plane_and_debris(gridlib, oracle, k):
 @pytest.mark.parametrize("frame", [0, 7])
 def test_deforming_sphere(gridlib, oracle, k, frame):
     sc = scenes.deforming_sphere(frame)
-    _check_grid(gridlib, oracle, sc.verts, sc.idx, k)
+    s, g = _check_grid(gridlib, oracle, sc.verts, sc.idx, k)
+    if k == 2:
+        # the pole cells exercise the warp shared-slice sort (33..256) and
+        # the block bitonic sort (257..4096)
+        counts = np.diff(g.offsets)
+        for lo, hi in ((33, 256), (257, 4096)):
+            assert ((counts >= lo) & (counts <= hi)).any(), (lo, hi)
 
 
 def test_skewed_density(gridlib, oracle):
     sc = scenes.skewed_density()
     s, g = _check_grid(gridlib, oracle, sc.verts, sc.idx, 4)
     counts = np.diff(g.offsets)
-    assert counts.max() > 4096   # exercises the large-cell sort
+    # per-cell sort classes: block bitonic (257..4096), block bitmap (>4096)
+    for lo, hi in ((2, 32), (257, 4096), (4097, 1 << 30)):
+        assert ((counts >= lo) & (counts <= hi)).any(), (lo, hi)
 
 
 def test_single_and_planar(gridlib, oracle):

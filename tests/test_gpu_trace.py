@@ -183,12 +183,12 @@ def test_heavy_cell_deferral_is_exact(gridlib, oracle, heavy):
     cam = scenes.deforming_sphere_camera(1024, 1024) if heavy == 1 else scenes.deforming_sphere_camera(512, 512)
     s.set_tuning(heavy_cell=0, cell_records=False)
     ref = _frame(s, cam)
-    for crec in (False, True):
-        s.set_tuning(heavy_cell=heavy, cell_records=crec)
+    for crec, lanes in ((False, 8), (True, 4), (True, 16), (False, 32)):
+        s.set_tuning(heavy_cell=heavy, cell_records=crec, heavy_lanes=lanes)
         s.build(8)
         out = _frame(s, cam)
         for a, b in zip(ref, out):
-            assert np.array_equal(a, b), (heavy, crec)
+            assert np.array_equal(a, b), (heavy, crec, lanes)
     # the nearest / any entry points on explicit rays agree as well
     rng = np.random.default_rng(11)
     rays = scenes.random_rays(rng, 50_000, (-1.2, -1.2, -1.2), (1.2, 1.2, 1.2))
