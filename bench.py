@@ -401,6 +401,12 @@ def run_gpu(args, rank, ws, local, dist):
     peak, peak_kind = _peaks()
     achieved = alg_bytes / kern_s / 1e9
     traffic = _traffic_from_profiles("trace_frame", alg_bytes)
+    l2_peak = _l2_copy_gbs(dev)
+    # build roofline: 12 N index bytes + 12 V vertex bytes + 4 (C + 1) offsets
+    # + 4 R ids per build, over the median device-timed build
+    gi = s.info()
+    build_bytes = 12 * ntris + 12 * nverts + 4 * (gi["ncells"] + 1) + 4 * gi["nrefs"]
+    build_s = head["build_ms"] / 1e3
 
     # e2e through the public C ABI with host buffers
     e2e = run_e2e(args, s, v, idx, nrm, cam, light, best_k, order, dist)
@@ -429,9 +435,17 @@ def run_gpu(args, rank, ws, local, dist):
                      "kernel": "trace_kernel camera + any, with their warp-per-ray passes when enabled "
                                "(one frame's trace launches)",
                      "alg_bytes_per_launch": int(alg_bytes),
-                     "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"])},
+                     "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"]),
+                     "l2": {"peak": round(l2_peak, 1), "frac": round(achieved / l2_peak, 4),
+                            "peak_source": "measured in this run: torch copy of a 32 MiB L2-resident buffer "
+                                           "(read + write bytes, best of 20 x 10 copies)"}},
+        "build_roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": peak,
+                           "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / peak, 4),
+                           "alg_bytes": int(build_bytes), "ms": head["build_ms"],
+                           "cells": int(gi["ncells"]), "refs": int(gi["nrefs"])},
         "cpu_baseline": {"value": round(cpu["rays"] / cpu["t_frame"] / 1e6, 4), "unit": "Mrays/s",
-                         "cores": cpu["threads"], "kind": "port",
+                         "cores": cpu["threads"], "kind": "port", "nproc": os.cpu_count(),
+                         "cpu_model": _cpu_model(),
                          "sample": f"10 of the 20 frames, k={best_k}: single-thread grid build (as the reference "
                                    f"builds) + all 1024^2 primary rays and their shadow rays on {cpu['threads']} "
                                    f"threads; value = rays / (build + trace) time",
@@ -442,6 +456,38 @@ def run_gpu(args, rank, ws, local, dist):
                    "reasons": clocks.get("reasons", []), "samples": clocks.get("samples", 0)},
     }
     print(json.dumps(out), flush=True)
+
+
+def _l2_copy_gbs(dev) -> float:
+    """Achievable L2 bandwidth: device-to-device copy of a 32 MiB buffer whose
+    source and destination (64 MiB) stay in the 126 MiB L2."""
+    import torch
+    a = torch.ones(8 << 20, dtype=torch.float32, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(5):
+        b.copy_(a)
+    best = float("inf")
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            b.copy_(a)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 10)
+    return 2 * a.numel() * 4 / (best / 1e3) / 1e9
+
+
+def _cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 def _traffic_from_profiles(kernel: str, alg_bytes: int):

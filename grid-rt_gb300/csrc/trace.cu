@@ -28,6 +28,12 @@ namespace gridrt {
 static constexpr unsigned FULL = 0xffffffffu;
 static constexpr int32_t kDeferred = -3;    // Lane::id of a ray handed to the warp-per-ray pass
 static constexpr int32_t kNoHeavy = 0x7fffffff;
+// A ray is also deferred once its tests would pass kHeavyWorkMult x the
+// heavy-cell threshold in total (0: only long lists defer).
+#ifndef GRIDRT_HEAVY_WORK_MULT
+#define GRIDRT_HEAVY_WORK_MULT 8
+#endif
+static constexpr int32_t kHeavyWorkMult = GRIDRT_HEAVY_WORK_MULT;
 
 static unsigned long long g_launches = 0;
 void count_launches(int n) { __atomic_add_fetch(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
@@ -69,6 +75,7 @@ struct Lane {
     float tMx, tMy, tMz, tDx, tDy, tDz;
     int32_t x, y, z;
     int32_t budget;
+    int32_t work;        // triangle tests made so far by this ray
     float best;
     int32_t id;
     int32_t cw;          // cached occupancy word index
@@ -114,6 +121,7 @@ __device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear
     // A walk visits at most nx+ny+nz-2 cells; the bound only guards against a
     // zero direction component (outside the reference's domain) looping.
     L.budget = P.res[0] + P.res[1] + P.res[2] + 3;
+    L.work = 0;
     L.best = kFltMax;
     L.id = -1;
     L.cw = -1;
@@ -175,7 +183,7 @@ template <int MODE, int ER>
 __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t* __restrict__ offsets,
                                         const int32_t* __restrict__ ids, const float4* __restrict__ tris,
                                         const uint32_t* __restrict__ occ, const float4* __restrict__ crec,
-                                        int32_t heavy, uint32_t& cells, uint32_t& tests) {
+                                        int32_t heavy, int32_t work_cap, uint32_t& cells, uint32_t& tests) {
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
     for (int s = 0; s < ER; ++s) {
         ++cells;
@@ -187,13 +195,15 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
         if (L.cword & occ_bit(L.x, L.y, L.z)) {
             const int32_t c = L.x + L.y * nx + L.z * nxy;
             const int32_t b = __ldg(offsets + c), e = __ldg(offsets + c + 1);
-            if (e - b > heavy) {
-                // long list: the ray goes to the warp-per-ray pass, which
-                // resumes the walk at this cell (and counts it)
+            if (e - b > heavy || L.work > work_cap - (e - b)) {
+                // a long list, or a ray that has made many tests already
+                // (grazing a surface): the ray goes to the deferred pass,
+                // which resumes the walk at this cell (and counts it)
                 --cells;
                 L.id = kDeferred;
                 return true;
             }
+            L.work += e - b;
             const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
             tests += (uint32_t)(e - b);
             int32_t i = b;
@@ -442,6 +452,8 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
     bool active = ray < io.n;
     L.ray = (int32_t)ray;
     int32_t heavy = io.heavy;
+    int32_t work_cap = heavy < kNoHeavy / (kHeavyWorkMult + 1) && kHeavyWorkMult > 0 ? heavy * kHeavyWorkMult
+                                                                                    : kNoHeavy;
     if (active) {
         ++started;
         if (!start_ray<MODE>(P, io, L, L.ray)) {
@@ -450,7 +462,8 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
         }
     }
     while (__any_sync(FULL, active)) {
-        bool fin = active && advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, s.crec, heavy, cells, tests);
+        bool fin = active &&
+                   advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, s.crec, heavy, work_cap, cells, tests);
         if (io.defer) {
             // warp-aggregated push of the lanes that met a long list
             const bool d = fin && L.id == kDeferred;
@@ -468,6 +481,7 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
                         active = false;
                     } else {
                         heavy = kNoHeavy;        // queue full: the lane tests the cell itself
+                        work_cap = kNoHeavy;
                         L.id = -1;
                     }
                     fin = false;
