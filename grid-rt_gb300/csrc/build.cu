@@ -683,21 +683,51 @@ __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offs
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
-    for (int64_t i = warp; i < nq; i += nwarps) {
-        const int32_t c = q[i];
-        const int32_t s = offsets[c], n = offsets[c + 1] - s;
-        int32_t v = lane < n ? ids[s + lane] : INT_MAX;
-#pragma unroll
-        for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                const int32_t o = __shfl_xor_sync(FULL, v, j);
-                const bool up = (lane & k) == 0;
-                const bool lower = (lane & j) == 0;
-                v = (lower == up) ? min(v, o) : max(v, o);
-            }
+    // a warp takes 32 queued cells: each lane sorts its own cell when it has
+    // at most 8 entries (19-comparator network in registers); the larger
+    // ones (9..32) are then sorted one after another by the whole warp
+    for (int64_t base = warp * 32; base < nq; base += nwarps * 32) {
+        const int64_t i = base + lane;
+        int32_t s = 0, n = 0;
+        if (i < nq) {
+            const int32_t c = q[i];
+            s = offsets[c];
+            n = offsets[c + 1] - s;
         }
-        if (lane < n) ids[s + lane] = v;
+        if (n <= 8) {
+            int32_t v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = k < n ? ids[s + k] : INT_MAX;
+#define GRIDRT_CX(a, b) { const int32_t lo_ = min(v[a], v[b]), hi_ = max(v[a], v[b]); v[a] = lo_; v[b] = hi_; }
+            GRIDRT_CX(0, 2) GRIDRT_CX(1, 3) GRIDRT_CX(4, 6) GRIDRT_CX(5, 7)
+            GRIDRT_CX(0, 4) GRIDRT_CX(1, 5) GRIDRT_CX(2, 6) GRIDRT_CX(3, 7)
+            GRIDRT_CX(0, 1) GRIDRT_CX(2, 3) GRIDRT_CX(4, 5) GRIDRT_CX(6, 7)
+            GRIDRT_CX(2, 4) GRIDRT_CX(3, 5)
+            GRIDRT_CX(1, 4) GRIDRT_CX(3, 6)
+            GRIDRT_CX(1, 2) GRIDRT_CX(3, 4) GRIDRT_CX(5, 6)
+#undef GRIDRT_CX
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (k < n) ids[s + k] = v[k];
+        }
+        unsigned big = __ballot_sync(FULL, n > 8);
+        while (big) {
+            const int src = __ffs(big) - 1;
+            big &= big - 1;
+            const int32_t cs = __shfl_sync(FULL, s, src), cn = __shfl_sync(FULL, n, src);
+            int32_t v = lane < cn ? ids[cs + lane] : INT_MAX;
+#pragma unroll
+            for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    const int32_t o = __shfl_xor_sync(FULL, v, j);
+                    const bool up = (lane & k) == 0;
+                    const bool lower = (lane & j) == 0;
+                    v = (lower == up) ? min(v, o) : max(v, o);
+                }
+            }
+            if (lane < cn) ids[cs + lane] = v;
+        }
     }
 }
 
@@ -924,7 +954,7 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     out[BK_TRI] = clampi((a.ntris + 255) / 256, 16 * sms);            // one warp per 32 triangles
     out[BK_TILE] = clampi((a.cell_cap + SCAN_TILE - 1) / SCAN_TILE, 8 * sms);
     out[BK_ONE] = 1;
-    out[BK_SSMALL] = clampi(a.cell_cap / 512 + 1, 8 * sms);
+    out[BK_SSMALL] = clampi(a.cell_cap / 4096 + 1, 8 * sms);            // 32 cells a warp
     out[BK_SMED] = clampi(a.cell_cap / 2048 + 1, 4 * sms);             // 16 warps a block, one cell a warp
     out[BK_SLARGE] = clampi(a.cell_cap / 16384 + 1, 2 * sms);
     out[BK_REFS] = a.crec ? clampi((a.ref_cap + 255) / 256, 16 * sms) : 0;

@@ -580,24 +580,40 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
             }
         }
         const unsigned trips = __reduce_max_sync(FULL, (unsigned)((e - b + G - 1) / G));
-        for (unsigned it = 0; it < trips; ++it) {
-            const int32_t i = b + gl + (int32_t)it * G;
-            if (i < e) {
-                int32_t tid;
-                float4 A, B, C;
-                if (s.crec) {
-                    A = __ldg(s.crec + 3 * (int64_t)i);
-                    B = __ldg(s.crec + 3 * (int64_t)i + 1);
-                    C = __ldg(s.crec + 3 * (int64_t)i + 2);
-                    tid = __float_as_int(A.w);
-                } else {
-                    tid = __ldg(s.ids + i);
-                    A = __ldg(s.tris + 3 * (int64_t)tid);
-                    B = __ldg(s.tris + 3 * (int64_t)tid + 1);
-                    C = __ldg(s.tris + 3 * (int64_t)tid + 2);
+        // two entries per lane and turn, both loaded before either is tested
+        for (unsigned it = 0; it < trips; it += 2) {
+            const int32_t i0 = b + gl + (int32_t)it * G, i1 = i0 + G;
+            int32_t t0 = -1, t1 = -1;
+            float4 A0, B0, C0, A1, B1, C1;
+            if (s.crec) {
+                if (i0 < e) {
+                    A0 = __ldg(s.crec + 3 * (int64_t)i0);
+                    B0 = __ldg(s.crec + 3 * (int64_t)i0 + 1);
+                    C0 = __ldg(s.crec + 3 * (int64_t)i0 + 2);
+                    t0 = __float_as_int(A0.w);
                 }
-                test_tri<MODE_NEAREST>(L, tid, A, B, C, hi);
+                if (i1 < e) {
+                    A1 = __ldg(s.crec + 3 * (int64_t)i1);
+                    B1 = __ldg(s.crec + 3 * (int64_t)i1 + 1);
+                    C1 = __ldg(s.crec + 3 * (int64_t)i1 + 2);
+                    t1 = __float_as_int(A1.w);
+                }
+            } else {
+                if (i0 < e) t0 = __ldg(s.ids + i0);
+                if (i1 < e) t1 = __ldg(s.ids + i1);
+                if (t0 >= 0) {
+                    A0 = __ldg(s.tris + 3 * (int64_t)t0);
+                    B0 = __ldg(s.tris + 3 * (int64_t)t0 + 1);
+                    C0 = __ldg(s.tris + 3 * (int64_t)t0 + 2);
+                }
+                if (t1 >= 0) {
+                    A1 = __ldg(s.tris + 3 * (int64_t)t1);
+                    B1 = __ldg(s.tris + 3 * (int64_t)t1 + 1);
+                    C1 = __ldg(s.tris + 3 * (int64_t)t1 + 2);
+                }
             }
+            if (t0 >= 0) test_tri<MODE_NEAREST>(L, t0, A0, B0, C0, hi);
+            if (t1 >= 0) test_tri<MODE_NEAREST>(L, t1, A1, B1, C1, hi);
         }
 #pragma unroll
         for (int o = G >> 1; o > 0; o >>= 1) {
