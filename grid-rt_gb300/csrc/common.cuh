@@ -66,7 +66,7 @@ __device__ __forceinline__ void raise_status(GridParams* p, BuildWork* w, uint32
     if (w) atomicOr(&w->sticky, bits);
 }
 
-static __device__ __forceinline__ bool build_failed(uint32_t s) {
+static __host__ __device__ __forceinline__ bool build_failed(uint32_t s) {
     return (s & (ST_CELL_CAP | ST_AMBIGUOUS | ST_TOO_BIG | ST_REF_CAP | ST_SORT_CAP | ST_BAD_RANGE)) != 0;
 }
 

@@ -122,6 +122,26 @@ struct BatchTask {
 void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
                         const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st);
 
+// Two-level instancing: one entry per instance, in trace order.
+struct InstanceRec {
+    SceneView view;
+    float xf[12];          // local_from_world, 3 x 4 row-major (applied to rays)
+    int32_t skip;          // empty or failed grid: never hit
+    int32_t pad[3];
+};
+struct InstanceBox {
+    float bmin[3], bmax[3];   // scene box: union of the instances' world boxes
+};
+// Device bytes of the per-instance grid-parameter table the launcher fills.
+size_t instance_params_bytes(int ninst);
+// mode 0: closest hit into hits (+ instance index into inst_out when not
+// null); mode 1: occlusion into occ.  Launches a parameter-table kernel and
+// the trace.
+void launch_trace_instances(const InstanceRec* recs, void* d_params, int ninst, const InstanceBox& box,
+                            const float4* rays, int64_t n, int4* hits, int32_t* inst_out, uint8_t* occ, int mode,
+                            TraceCounters* ctr, unsigned long long* counter, const TraceTuning& tune, int num_sms,
+                            cudaStream_t st);
+
 void launch_deform(const float* base, const float* normals, float* out, int64_t nverts, float amp, float freq,
                    float phase, cudaStream_t st);
 

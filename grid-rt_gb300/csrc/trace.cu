@@ -239,8 +239,11 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
                              C0 = __ldg(tris + 3 * (int64_t)t0 + 2);
                 if (test_tri<MODE>(L, t0, A0, B0, C0, hi)) return true;
             }
-            if (L.best < kFltMax) {
-                // any-hit: the first cell with a hit decides -- here not before tmax
+            if (L.id >= 0) {
+                // a hit closer than the best on entry (the one-geometry walk
+                // starts from FLT_MAX; an instance walk from the instances
+                // before it).  Any-hit: the first cell with a hit decides --
+                // here not before tmax
                 if (MODE == MODE_ANY) L.id = -1;
                 return true;
             }
@@ -779,6 +782,190 @@ __global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene*
             if (any) finish_ray<MODE_ANY>(io, P[scene], V.tris, L);
             else finish_ray<MODE_NEAREST>(io, P[scene], V.tris, L);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// two-level instancing: IAccStruct::traceNearestInstance
+// (src/rtcore/IAccStruct.cpp:26-72).  The ray is clipped against the scene
+// box (union of the instances' world boxes); then, instance by instance in
+// order, the ray taken to the instance's local space (same tnear / tfar,
+// direction not renormalised, so t is the same in both spaces) walks that
+// instance's grid starting from the best distance so far: a later instance
+// wins only with a strictly closer hit.  Matrix rows are applied as
+// x' = ((m0 x + m1 y) + m2 z) + m3, one rounding per operation.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void xf_point(const float* m, float x, float y, float z, float& ox, float& oy, float& oz) {
+    ox = fadd(fadd(fadd(fmul(m[0], x), fmul(m[1], y)), fmul(m[2], z)), m[3]);
+    oy = fadd(fadd(fadd(fmul(m[4], x), fmul(m[5], y)), fmul(m[6], z)), m[7]);
+    oz = fadd(fadd(fadd(fmul(m[8], x), fmul(m[9], y)), fmul(m[10], z)), m[11]);
+}
+
+__device__ __forceinline__ void xf_dir(const float* m, float x, float y, float z, float& ox, float& oy, float& oz) {
+    ox = fadd(fadd(fmul(m[0], x), fmul(m[1], y)), fmul(m[2], z));
+    oy = fadd(fadd(fmul(m[4], x), fmul(m[5], y)), fmul(m[6], z));
+    oz = fadd(fadd(fmul(m[8], x), fmul(m[9], y)), fmul(m[10], z));
+}
+
+__global__ void instances_prep_kernel(const InstanceRec* __restrict__ recs, int ninst, SParams* __restrict__ sp) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ninst; i += gridDim.x * blockDim.x)
+        fill_sparams(recs[i].view.params, sp[i]);
+}
+
+template <int MODE, int ER>
+__global__ void __launch_bounds__(128) trace_instances_kernel(const InstanceRec* __restrict__ recs,
+                                                              const SParams* __restrict__ sp, int ninst,
+                                                              InstanceBox box, TraceIO io, int32_t* inst_out) {
+    __shared__ SParams Pw[4];
+    const int lane = threadIdx.x & 31;
+    SParams& P = Pw[threadIdx.x >> 5];
+    uint32_t cells = 0, tests = 0, started = 0;
+    for (;;) {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(io.counter, 32ull);
+        b = __shfl_sync(FULL, b, 0);
+        if ((long long)b >= io.n) break;
+        const long long r = (long long)b + lane;
+        bool alive = r < io.n, noray = false;
+        float wo[3] = {0.f, 0.f, 0.f}, wd[3] = {1.f, 1.f, 1.f};
+        float tn = 0.f, tf = 0.f, tmax = 0.f;
+        if (alive) {
+            ++started;
+            const float4 a = __ldg(io.rays + 2 * r), c = __ldg(io.rays + 2 * r + 1);
+            wo[0] = a.x; wo[1] = a.y; wo[2] = a.z;
+            wd[0] = c.x; wd[1] = c.y; wd[2] = c.z;
+            tn = a.w;
+            tf = tmax = c.w;
+            if (MODE == MODE_ANY && tf < 0.0f) {
+                noray = true;
+                alive = false;
+            } else {
+                // Ray::update + AabbIntersection::clipRay on the scene box
+                float rn = tn, rf = tf;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float inv = frcp(wd[d]);
+                    const float t0 = fmul(fsub(box.bmin[d], wo[d]), inv), t1 = fmul(fsub(box.bmax[d], wo[d]), inv);
+                    rn = vmax(rn, vmin(t0, t1));
+                    rf = vmin(rf, vmax(t0, t1));
+                }
+                if (rn > rf) alive = false;
+                tn = rn;
+                tf = rf;
+            }
+        }
+        float gbest = kFltMax;
+        int32_t gid = -1, ginst = -1;
+        for (int i = 0; i < ninst; ++i) {
+            if (!__any_sync(FULL, alive)) break;
+            __syncwarp();
+            {
+                const uint32_t* src = reinterpret_cast<const uint32_t*>(sp + i);
+                uint32_t* dst = reinterpret_cast<uint32_t*>(&P);
+                for (int w = lane; w < (int)(sizeof(SParams) / 4); w += 32) dst[w] = __ldg(src + w);
+            }
+            __syncwarp();
+            const InstanceRec* R = recs + i;
+            Lane L;
+            bool active = alive && !P.failed && !__ldg(&R->skip);
+            if (active) {
+                float m[12];
+#pragma unroll
+                for (int k = 0; k < 12; ++k) m[k] = __ldg(&R->xf[k]);
+                xf_point(m, wo[0], wo[1], wo[2], L.ox, L.oy, L.oz);
+                xf_dir(m, wd[0], wd[1], wd[2], L.dx, L.dy, L.dz);
+                active = setup_ray(P, L, tn, tf);
+                L.tmax = tmax;
+                if (MODE == MODE_NEAREST) L.best = gbest;
+            }
+            const int32_t* offs = R->view.offsets;
+            const int32_t* ids = R->view.ids;
+            const float4* tris = R->view.tris;
+            const uint32_t* occ = R->view.occ;
+            const float4* crec = R->view.crec;
+            while (__any_sync(FULL, active)) {
+                if (active && advance<MODE, ER>(P, L, offs, ids, tris, occ, crec, kNoHeavy, kNoHeavy, cells, tests)) {
+                    active = false;
+                    if (L.id >= 0) {
+                        gbest = L.best;
+                        gid = L.id;
+                        ginst = i;
+                        if (MODE == MODE_ANY) alive = false;   // occluded
+                    }
+                }
+            }
+        }
+        if (r < io.n) {
+            if (MODE == MODE_ANY) {
+                io.occ[r] = noray ? 2 : (gid >= 0 ? 1 : 0);
+            } else {
+                int4 h = make_int4(-1, 0, 0, 0);
+                if (gid >= 0) {
+                    // reported values in the winning instance's space
+                    const InstanceRec* R = recs + ginst;
+                    float m[12];
+#pragma unroll
+                    for (int k = 0; k < 12; ++k) m[k] = __ldg(&R->xf[k]);
+                    Lane L;
+                    xf_point(m, wo[0], wo[1], wo[2], L.ox, L.oy, L.oz);
+                    xf_dir(m, wd[0], wd[1], wd[2], L.dx, L.dy, L.dz);
+                    L.id = gid;
+                    L.best = gbest;
+                    h = refined_hit(R->view.tris, L);
+                }
+                io.hits[r] = h;
+                if (inst_out) inst_out[r] = ginst;
+            }
+        }
+    }
+    if (io.ctr) flush_counters(io.ctr, started, cells, tests);
+}
+
+template <int MODE, int ER>
+static void launch_instances_er(const InstanceRec* recs, const SParams* sp, int ninst, const InstanceBox& box,
+                                const TraceIO& io, int32_t* inst_out, const TraceTuning& tune, int num_sms,
+                                cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_instances_kernel<MODE, ER>, 128, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    long long blocks = (io.n + 127) / 128;
+    if (tune.persistent) blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
+    trace_instances_kernel<MODE, ER><<<(int)blocks, 128, 0, st>>>(recs, sp, ninst, box, io, inst_out);
+}
+
+size_t instance_params_bytes(int ninst) { return sizeof(SParams) * (size_t)(ninst > 0 ? ninst : 1); }
+
+void launch_trace_instances(const InstanceRec* recs, void* d_params, int ninst, const InstanceBox& box,
+                            const float4* rays, int64_t n, int4* hits, int32_t* inst_out, uint8_t* occ, int mode,
+                            TraceCounters* ctr, unsigned long long* counter, const TraceTuning& tune, int num_sms,
+                            cudaStream_t st) {
+    if (n <= 0 || ninst <= 0) return;
+    count_launches(2);
+    SParams* sp = static_cast<SParams*>(d_params);
+    instances_prep_kernel<<<(ninst + 127) / 128, 128, 0, st>>>(recs, ninst, sp);
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    TraceIO io{};
+    io.rays = rays;
+    io.hits = hits;
+    io.occ = occ;
+    io.n = n;
+    io.counter = counter;
+    io.ctr = ctr;
+    io.heavy = kNoHeavy;
+    const int er = tune.empty_run;
+    if (mode == MODE_ANY) {
+        if (er <= 2) launch_instances_er<MODE_ANY, 2>(recs, sp, ninst, box, io, inst_out, tune, num_sms, st);
+        else if (er <= 4) launch_instances_er<MODE_ANY, 4>(recs, sp, ninst, box, io, inst_out, tune, num_sms, st);
+        else launch_instances_er<MODE_ANY, 8>(recs, sp, ninst, box, io, inst_out, tune, num_sms, st);
+    } else {
+        if (er <= 2) launch_instances_er<MODE_NEAREST, 2>(recs, sp, ninst, box, io, inst_out, tune, num_sms, st);
+        else if (er <= 4) launch_instances_er<MODE_NEAREST, 4>(recs, sp, ninst, box, io, inst_out, tune, num_sms, st);
+        else launch_instances_er<MODE_NEAREST, 8>(recs, sp, ninst, box, io, inst_out, tune, num_sms, st);
     }
 }
 

@@ -66,6 +66,10 @@ class ServeOptionsC(C.Structure):
                 ("plain", C.c_int32), ("empty_run", C.c_int32), ("pad", C.c_int32)]
 
 
+class InstanceC(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("world_from_local", C.c_float * 12), ("local_from_world", C.c_float * 12)]
+
+
 class CameraC(C.Structure):
     _fields_ = [("eye", C.c_float * 3), ("base_dir", C.c_float * 3), ("near_u", C.c_float * 3),
                 ("near_v", C.c_float * 3), ("width", C.c_int32), ("height", C.c_int32), ("order", C.c_int32),
@@ -95,6 +99,9 @@ EXPORTS = [
     "rtg_scene_set_tuning", "rtg_scene_counters", "rtg_batch_create", "rtg_batch_build_async",
     "rtg_batch_trace_async", "rtg_batch_check", "rtg_batch_rays", "rtg_batch_set_tuning", "rtg_batch_destroy",
     "rtg_serve_run",
+    "rtg_instances_create", "rtg_instances_update", "rtg_instances_box", "rtg_instances_set_tuning",
+    "rtg_trace_nearest_instances_device", "rtg_trace_any_instances_device", "rtg_trace_nearest_instances",
+    "rtg_instances_destroy",
 ]
 
 
@@ -157,6 +164,14 @@ def load(build_if_missing: bool = True):
         "rtg_serve_run": ([C.POINTER(vp), i32, C.POINTER(RequestC), i64, C.POINTER(ServeOptionsC),
                            C.POINTER(RequestTimesC)], C.c_int),
         "rtg_scene_counters": ([vp, C.POINTER(C.c_int64), C.c_int], C.c_int),
+        "rtg_instances_create": ([C.POINTER(InstanceC), i32, C.POINTER(vp)], C.c_int),
+        "rtg_instances_update": ([vp, C.POINTER(InstanceC), i32], C.c_int),
+        "rtg_instances_box": ([vp, vp, vp], C.c_int),
+        "rtg_instances_set_tuning": ([vp, i32, i32], C.c_int),
+        "rtg_trace_nearest_instances_device": ([vp, vp, i64, vp, vp, i32, vp], C.c_int),
+        "rtg_trace_any_instances_device": ([vp, vp, i64, vp, i32, vp], C.c_int),
+        "rtg_trace_nearest_instances": ([vp, vp, i64, vp, vp, vp], C.c_int),
+        "rtg_instances_destroy": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -336,6 +351,69 @@ class Scene:
 
 RTG_MODE_NEAREST = 0
 RTG_MODE_ANY = 1
+
+
+def _instance_structs(items):
+    arr = (InstanceC * len(items))()
+    for i, (scene, xf, inv) in enumerate(items):
+        arr[i].scene = scene.h
+        xf = np.ascontiguousarray(xf, np.float32).reshape(12)
+        inv = np.ascontiguousarray(inv, np.float32).reshape(12)
+        for k in range(12):
+            arr[i].world_from_local[k] = float(xf[k])
+            arr[i].local_from_world[k] = float(inv[k])
+    return arr
+
+
+class Instances:
+    """Ordered instance set over built scenes: (Scene, world_from_local 3x4,
+    local_from_world 3x4) triples (rtg_instances_*)."""
+
+    def __init__(self, items):
+        self.items = list(items)
+        h = C.c_void_p()
+        arr = _instance_structs(self.items)
+        check(load().rtg_instances_create(arr, len(self.items), C.byref(h)))
+        self.h = h
+
+    def update(self, items):
+        self.items = list(items)
+        arr = _instance_structs(self.items)
+        check(load().rtg_instances_update(self.h, arr, len(self.items)))
+
+    def boxes(self):
+        box = np.empty(6, np.float32)
+        inst = np.empty((len(self.items), 6), np.float32)
+        check(load().rtg_instances_box(self.h, _ptr(box), _ptr(inst)))
+        return box, inst
+
+    def set_tuning(self, empty_run: int = None, persistent: bool = None):
+        if empty_run is not None:
+            check(load().rtg_instances_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
+        if persistent is not None:
+            check(load().rtg_instances_set_tuning(self.h, RTG_TUNE_PERSISTENT, 1 if persistent else 0))
+
+    def trace_nearest(self, rays: np.ndarray):
+        """Host rays -> (n x 4 hit words, instance index per ray)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        hits = np.empty((n, 4), np.float32)
+        inst = np.empty(n, np.int32)
+        check(load().rtg_trace_nearest_instances(self.h, _ptr(rays), n, _ptr(hits), _ptr(inst), None))
+        return hits, inst
+
+    def trace_nearest_device(self, d_rays, n: int, d_hits, d_inst=None, stream=None):
+        check(load().rtg_trace_nearest_instances_device(self.h, _ptr(d_rays), int(n), _ptr(d_hits),
+                                                        _ptr(d_inst) if d_inst is not None else None, 0, stream))
+
+    def trace_any_device(self, d_rays, n: int, d_occ, stream=None):
+        check(load().rtg_trace_any_instances_device(self.h, _ptr(d_rays), int(n), _ptr(d_occ), 0, stream))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and _lib is not None:
+            _lib.rtg_instances_destroy(h)
+            self.h = None
 
 
 class Batch:

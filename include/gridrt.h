@@ -268,6 +268,48 @@ rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
 rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
 rtg_status rtg_batch_destroy(rtg_batch batch);
 
+/* ---- two-level instancing -------------------------------------------------
+ * The scene level of the reference's plugin interface: an ordered set of
+ * instances, each a built scene placed by a 3 x 4 row-major matrix.
+ *   rtg_instances_create   Context::instantiateGeometry for every instance +
+ *                          IAccStructBuilder::buildInstance (src/rtcore/Context.cpp:352-390,
+ *                          src/rtcore/IAccStructBuilder.cpp:16-33): world box of each
+ *                          instance (its grid box's corners transformed, 1% enlarged) and
+ *                          the scene box over all of them
+ *   rtg_trace_nearest_instances*  IAccStruct::traceNearestInstance
+ *                          (src/rtcore/IAccStruct.cpp:26-72): the ray is clipped against the
+ *                          scene box, then taken to each instance's local space in order
+ *                          (origin by local_from_world, direction by its 3 x 3 part, not
+ *                          renormalised) and traced from the best distance so far, so a
+ *                          later instance wins only with a strictly closer hit
+ *   rtg_trace_any_instances_device  occlusion: closest hit over all instances before
+ *                          the ray's tfar word (the reference's any-hit is a stub)
+ * Rows are applied as x' = ((m0 x + m1 y) + m2 z) + m3, one float rounding per
+ * operation.  The instance boxes are taken at create / update: call
+ * rtg_instances_update after rebuilding a member scene.  d_instance receives
+ * the winning instance's index (-1 on a miss); t is the same in world and
+ * local space, u / v are barycentrics of the local triangle. */
+typedef struct rtg_instances_s* rtg_instances;
+typedef struct {
+    rtg_scene scene;              /* built scene */
+    float world_from_local[12];   /* 3 x 4 row-major */
+    float local_from_world[12];   /* its inverse, applied to rays */
+} rtg_instance;
+rtg_status rtg_instances_create(const rtg_instance* inst, int32_t n, rtg_instances* out);
+rtg_status rtg_instances_update(rtg_instances set, const rtg_instance* inst, int32_t n);
+/* box: scene box {min xyz, max xyz}; inst_boxes (optional): 6 floats per instance. */
+rtg_status rtg_instances_box(rtg_instances set, float box[6], float* inst_boxes);
+/* Keys RTG_TUNE_EMPTY_RUN (2, 4, 8) and RTG_TUNE_PERSISTENT. */
+rtg_status rtg_instances_set_tuning(rtg_instances set, int32_t key, int32_t value);
+rtg_status rtg_trace_nearest_instances_device(rtg_instances set, const float* d_rays, int64_t n, rtg_hit* d_hits,
+                                              int32_t* d_instance, int32_t flags, void* stream);
+rtg_status rtg_trace_any_instances_device(rtg_instances set, const float* d_rays, int64_t n, uint8_t* d_occ,
+                                          int32_t flags, void* stream);
+/* Host arrays; instance (optional) receives the winning instance per ray. */
+rtg_status rtg_trace_nearest_instances(rtg_instances set, const float* rays, int64_t n, rtg_hit* hits,
+                                       int32_t* instance, void* stream);
+rtg_status rtg_instances_destroy(rtg_instances set);
+
 /* ---- serving: continuous batching over resident scenes ------------------
  * rtg_serve_run replays a stream of ray-query requests in real time against
  * built, resident scenes (up to 64, one device) and reports, per request, when

@@ -9,6 +9,8 @@
 //   rt::IAccStruct::traceNearestGeometry / traceAnyGeometry include/rt/IAccStruct.h:10-32
 //   rtp::UniformGridAccStructBuilder / UniformGridAccStruct (the grid plugin pair)
 //       include/rtp/UniformGridAccStructBuilder.h, include/rtp/UniformGridAccStruct.h
+//   the scene level, rtp::InstancedScene: IAccStructBuilder::buildInstance +
+//       IAccStruct::traceNearestInstance (include/rt/IAccStructBuilder.h:17, include/rt/IAccStruct.h:19)
 // Error behaviour follows the reference: the calls return void and fail
 // silently (a failed build leaves an acceleration structure that reports no
 // hits); lastStatus() exposes the rtg_status of the last C-ABI call.
@@ -63,8 +65,12 @@ struct Geometry {
     std::shared_ptr<IAccStruct> accStruct;
 };
 
+// rt::Instance with rt::Transform's two matrices (include/rt/Instance.h:13-18,
+// include/rt/Transform.h:10-29) as 3 x 4 row-major arrays.
 struct Instance {
     Geometry* geometry = nullptr;
+    float worldFromLocal[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+    float localFromWorld[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
 };
 
 class IAccStruct {
@@ -192,6 +198,71 @@ public:
 private:
     int32_t _k;
     int _device;
+    rtg_status _status = RTG_OK;
+};
+
+// The scene level: IAccStructBuilder::buildInstance + IAccStruct::traceNearestInstance
+// (src/rtcore/IAccStructBuilder.cpp:16-33, src/rtcore/IAccStruct.cpp:26-72) over
+// instances whose geometries were built by UniformGridAccStructBuilder.
+class InstancedScene {
+public:
+    InstancedScene() = default;
+    ~InstancedScene() { rtg_instances_destroy(_set); }
+    InstancedScene(const InstancedScene&) = delete;
+    InstancedScene& operator=(const InstancedScene&) = delete;
+
+    rtg_status lastStatus() const { return _status; }
+
+    void buildInstance(const std::vector<rt::Instance>& instances) {
+        _instances = instances;
+        std::vector<rtg_instance> v(instances.size());
+        for (size_t i = 0; i < instances.size(); ++i) {
+            auto* acc = dynamic_cast<UniformGridAccStruct*>(instances[i].geometry->accStruct.get());
+            if (!acc) {
+                _status = RTG_NOT_BUILT;
+                return;
+            }
+            v[i].scene = acc->scene();
+            for (int k = 0; k < 12; ++k) {
+                v[i].world_from_local[k] = instances[i].worldFromLocal[k];
+                v[i].local_from_world[k] = instances[i].localFromWorld[k];
+            }
+        }
+        rtg_instances_destroy(_set);
+        _set = nullptr;
+        _status = rtg_instances_create(v.data(), (int32_t)v.size(), &_set);
+    }
+
+    // traceNearestInstance for a batch of rays: hits[i].instance points into
+    // the vector given to buildInstance.
+    void traceNearestInstance(std::vector<rt::Ray>& rays, std::vector<rt::Hit>& hits) {
+        std::vector<float> r(rays.size() * 8);
+        for (size_t i = 0; i < rays.size(); ++i) {
+            const rt::Ray& q = rays[i];
+            float* o = &r[8 * i];
+            o[0] = q.orig.x; o[1] = q.orig.y; o[2] = q.orig.z; o[3] = q.tnear;
+            o[4] = q.dir.x; o[5] = q.dir.y; o[6] = q.dir.z; o[7] = q.tfar;
+        }
+        std::vector<rtg_hit> h(rays.size());
+        std::vector<int32_t> inst(rays.size());
+        hits.assign(rays.size(), rt::Hit());
+        _status = rtg_trace_nearest_instances(_set, r.data(), (int64_t)rays.size(), h.data(), inst.data(), nullptr);
+        if (_status != RTG_OK) return;
+        for (size_t i = 0; i < rays.size(); ++i) {
+            if (h[i].id < 0) continue;
+            rt::Hit& o = hits[i];
+            o.triangleId = (uint32_t)h[i].id;
+            o.distance = h[i].t;
+            o.v1Coord = h[i].u;
+            o.v2Coord = h[i].v;
+            o.v0Coord = 1.0f - h[i].u - h[i].v;
+            o.instance = &_instances[inst[i]];
+        }
+    }
+
+private:
+    std::vector<rt::Instance> _instances;
+    rtg_instances _set = nullptr;
     rtg_status _status = RTG_OK;
 };
 

@@ -279,8 +279,18 @@ static inline void hit_wald(const float* a, const oray* r, ohit* h, float* best)
  * src/rtplugins/UniformGridAccStruct.cpp:30-42, 113-196, 362-378.
  * Returns 1 with *t_out / *h on a hit.  cells/tests count the loop iterations
  * and Wald tests (for the algorithmic-bytes figure). */
+static int trace_one_from(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc,
+                          oray* r, ohit* h, float* t_out, int64_t* cells, int64_t* tests, float hit_distance);
+
 static int trace_one(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc, oray* r,
                      ohit* h, float* t_out, int64_t* cells, int64_t* tests) {
+    return trace_one_from(g, offsets, ids, acc, r, h, t_out, cells, tests, FLT_MAX);
+}
+
+/* hit_distance: the caller's best so far (Hit::distance on entry, which the
+ * reference carries from one instance to the next). */
+static int trace_one_from(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc,
+                          oray* r, ohit* h, float* t_out, int64_t* cells, int64_t* tests, float hit_distance) {
     if (!clip_ray(g, r)) return 0;
     const int32_t nx = g->res[0], ny = g->res[1], nz = g->res[2];
     float sp[3];
@@ -301,7 +311,6 @@ static int trace_one(const orc_grid_info* g, const int32_t* offsets, const int32
     float tMaxX = (voxel_to_world(g, x + !r->sbit[0], 0) - r->orig[0]) * r->inv[0];
     float tMaxY = (voxel_to_world(g, y + !r->sbit[1], 1) - r->orig[1]) * r->inv[1];
     float tMaxZ = (voxel_to_world(g, z + !r->sbit[2], 2) - r->orig[2]) * r->inv[2];
-    const float hit_distance = FLT_MAX;
     float best = hit_distance;
     do {
         const int64_t c = (int64_t)x + (int64_t)y * nx + (int64_t)z * nx * ny;
@@ -419,5 +428,135 @@ void orc_mt_f64(const float* verts, const int32_t* idx, const float* rays, const
         o[1] = (tv[0] * p[0] + tv[1] * p[1] + tv[2] * p[2]) * inv;
         o[2] = (d[0] * qv[0] + d[1] * qv[1] + d[2] * qv[2]) * inv;
         o[0] = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) * inv;
+    }
+}
+
+
+/* ---- two-level instancing ------------------------------------------------
+ * vr::mat4f (vrbase) is not vendored, so the matrix-vector product is
+ * restated with one fixed evaluation order, shared with the GPU library:
+ *   x' = ((m[0] x + m[1] y) + m[2] z) + m[3]   (rows of a 3 x 4 matrix)
+ * and directions drop the translation column (Transform::inverseTransform,
+ * include/rt/Transform.h:31-40). */
+static inline void xf_point(const float* m, const float* p, float* o) {
+    for (int i = 0; i < 3; ++i) {
+        float a = m[4 * i] * p[0];
+        float b = m[4 * i + 1] * p[1];
+        float c = m[4 * i + 2] * p[2];
+        o[i] = ((a + b) + c) + m[4 * i + 3];
+    }
+}
+
+static inline void xf_dir(const float* m, const float* d, float* o) {
+    for (int i = 0; i < 3; ++i) {
+        float a = m[4 * i] * d[0];
+        float b = m[4 * i + 1] * d[1];
+        float c = m[4 * i + 2] * d[2];
+        o[i] = (a + b) + c;
+    }
+}
+
+/* Context::instantiateGeometry (src/rtcore/Context.cpp:366-389): the eight
+ * corners of the geometry's box (Aabb::computeVertices order,
+ * src/rtcore/Aabb.cpp:124-134) transformed by the instance matrix and added
+ * to a default box with Aabb::expandBy(vertex) (if / else-if per axis,
+ * src/rtcore/Aabb.cpp:37-53), then Aabb::scaleBy(0.01f) (:78-91). */
+void orc_instance_box(const float* gbmin, const float* gbmax, const float* xf, float* bmin, float* bmax) {
+    const float c[8][3] = {{gbmin[0], gbmin[1], gbmax[2]}, {gbmax[0], gbmin[1], gbmax[2]},
+                           {gbmax[0], gbmin[1], gbmin[2]}, {gbmin[0], gbmin[1], gbmin[2]},
+                           {gbmin[0], gbmax[1], gbmax[2]}, {gbmax[0], gbmax[1], gbmax[2]},
+                           {gbmax[0], gbmax[1], gbmin[2]}, {gbmin[0], gbmax[1], gbmin[2]}};
+    for (int d = 0; d < 3; ++d) {
+        bmin[d] = FLT_MAX;
+        bmax[d] = -FLT_MAX;
+    }
+    for (int v = 0; v < 8; ++v) {
+        float p[3];
+        xf_point(xf, c[v], p);
+        for (int d = 0; d < 3; ++d) {
+            if (p[d] < bmin[d]) bmin[d] = p[d];
+            else if (p[d] > bmax[d]) bmax[d] = p[d];
+        }
+    }
+    for (int d = 0; d < 3; ++d) {
+        float sc = (bmin[d] == bmax[d]) ? 0.01f : vabs(bmax[d] - bmin[d]) * 0.01f;
+        bmin[d] -= sc;
+        bmax[d] += sc;
+    }
+}
+
+/* IAccStructBuilder::buildInstance (src/rtcore/IAccStructBuilder.cpp:16-33):
+ * default box expanded by every instance box (Aabb::expandBy(Aabb),
+ * src/rtcore/Aabb.cpp:55-76). */
+void orc_scene_box(int32_t ninst, const float* inst_boxes, float* box) {
+    for (int d = 0; d < 3; ++d) {
+        box[d] = FLT_MAX;
+        box[3 + d] = -FLT_MAX;
+    }
+    for (int32_t i = 0; i < ninst; ++i) {
+        for (int d = 0; d < 3; ++d) {
+            if (inst_boxes[6 * i + d] < box[d]) box[d] = inst_boxes[6 * i + d];
+            if (inst_boxes[6 * i + 3 + d] > box[3 + d]) box[3 + d] = inst_boxes[6 * i + 3 + d];
+        }
+    }
+}
+
+/* IAccStruct::traceNearestInstance (src/rtcore/IAccStruct.cpp:26-72): clip
+ * the ray against the scene box; then, instance by instance in order, trace
+ * the ray taken to the instance's local space (same tnear / tfar, direction
+ * not renormalised) with the best distance so far, so a later instance wins
+ * only with a strictly closer hit.  t is the same in both spaces (affine map).
+ * The ray's own tnear / tfar words stand for the Context's initialisation
+ * (tnear = ray epsilon, tfar = MAX, :34-36).  any != 0: occluded[i] = closest
+ * t < the ray's tfar word, as for a single geometry. */
+void orc_trace_instances(int32_t ninst, const orc_grid_info* const* g, const int32_t* const* offsets,
+                         const int32_t* const* ids, const float* const* acc, const float* inv, const float* box,
+                         const float* rays, int64_t n, float* hits, int32_t* inst_out, uint8_t* occluded,
+                         int nthreads) {
+    orc_grid_info sb;
+    memset(&sb, 0, sizeof(sb));
+    for (int d = 0; d < 3; ++d) {
+        sb.bmin[d] = box[d];
+        sb.bmax[d] = box[3 + d];
+    }
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+#endif
+    for (int64_t i = 0; i < n; ++i) {
+        oray w;
+        load_ray(rays + 8 * i, &w);
+        const float tmax = rays[8 * i + 7];
+        float best = FLT_MAX;
+        int32_t found = -1;
+        ohit hit = {-1, 0.f, 0.f};
+        if (clip_ray(&sb, &w)) {
+            for (int32_t j = 0; j < ninst; ++j) {
+                if (g[j]->ncells <= 0) continue;
+                oray r;
+                xf_point(inv + 12 * j, w.orig, r.orig);
+                xf_dir(inv + 12 * j, w.dir, r.dir);
+                r.tnear = w.tnear;
+                r.tfar = w.tfar;
+                ray_update(&r);
+                ohit h = {-1, 0.f, 0.f};
+                float t = 0.f;
+                if (trace_one_from(g[j], offsets[j], ids[j], acc[j], &r, &h, &t, NULL, NULL, best)) {
+                    best = t;
+                    found = j;
+                    hit = h;
+                }
+            }
+        }
+        if (occluded) occluded[i] = (uint8_t)(found >= 0 && best < tmax);
+        if (hits) {
+            float* o = hits + 4 * i;
+            const int32_t id = found >= 0 ? hit.id : -1;
+            memcpy(&o[0], &id, 4);
+            o[1] = found >= 0 ? best : 0.f;
+            o[2] = found >= 0 ? hit.u : 0.f;
+            o[3] = found >= 0 ? hit.v : 0.f;
+        }
+        if (inst_out) inst_out[i] = found;
     }
 }

@@ -63,6 +63,19 @@ void orc_trace_any(const orc_grid_info* g, const int32_t* offsets, const int32_t
 void orc_mt_f64(const float* verts, const int32_t* idx, const float* rays, const int32_t* tri, int64_t n,
                 double* out);
 
+/* Two-level instancing (see oracle.c): xf / inv are 3 x 4 row-major
+ * world_from_local / local_from_world matrices.  orc_instance_box gives an
+ * instance's world box from its geometry's grid box, orc_scene_box the union
+ * of ninst instance boxes (6 floats each: min xyz, max xyz). */
+void orc_instance_box(const float* gbmin, const float* gbmax, const float* xf, float* bmin, float* bmax);
+void orc_scene_box(int32_t ninst, const float* inst_boxes, float* box);
+/* hits (n x 4 words) / inst_out (instance index, -1 = miss) / occluded may be
+ * NULL independently. */
+void orc_trace_instances(int32_t ninst, const orc_grid_info* const* g, const int32_t* const* offsets,
+                         const int32_t* const* ids, const float* const* acc, const float* inv, const float* box,
+                         const float* rays, int64_t n, float* hits, int32_t* inst_out, uint8_t* occluded,
+                         int nthreads);
+
 /* Number of OpenMP threads the trace entry points use when nthreads <= 0. */
 int orc_max_threads(void);
 

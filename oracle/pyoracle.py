@@ -67,6 +67,10 @@ def lib():
                                     C.c_void_p, C.c_int]
         L.orc_mt_f64.argtypes = [_f32p, _i32p, _f32p, _i32p, C.c_int64, _f64p]
         L.orc_max_threads.restype = C.c_int
+        L.orc_instance_box.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p]
+        L.orc_scene_box.argtypes = [C.c_int32, _f32p, _f32p]
+        L.orc_trace_instances.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _f32p, _f32p,
+                                          _f32p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -120,6 +124,47 @@ class Grid:
         lib().orc_trace_any(C.byref(self.info), self.offsets, self.ids_padded, self.acc.ravel(), rays.ravel(), n,
                             occ, cnt.ctypes.data if counters else None, int(nthreads))
         return (occ, cnt) if counters else occ
+
+
+class Instances:
+    """Oracle instance set: (Grid, world_from_local 3x4, local_from_world 3x4)
+    triples, restating Context::instantiateGeometry, buildInstance and
+    traceNearestInstance (see oracle.c)."""
+
+    def __init__(self, items):
+        self.items = [(g, np.ascontiguousarray(xf, np.float32).reshape(12), np.ascontiguousarray(inv, np.float32)
+                       .reshape(12)) for g, xf, inv in items]
+        L = lib()
+        n = len(self.items)
+        self.boxes = np.empty((n, 6), np.float32)
+        for i, (g, xf, _) in enumerate(self.items):
+            bmin = np.ascontiguousarray(g.info.bmin, np.float32)
+            bmax = np.ascontiguousarray(g.info.bmax, np.float32)
+            lo = np.empty(3, np.float32)
+            hi = np.empty(3, np.float32)
+            L.orc_instance_box(bmin, bmax, xf, lo, hi)
+            self.boxes[i, :3] = lo
+            self.boxes[i, 3:] = hi
+        self.box = np.empty(6, np.float32)
+        L.orc_scene_box(n, self.boxes.ravel(), self.box)
+        self._g = (C.POINTER(GridInfo) * n)(*[C.pointer(g.info) for g, _, _ in self.items])
+        self._off = (C.c_void_p * n)(*[g.offsets.ctypes.data for g, _, _ in self.items])
+        self._ids = (C.c_void_p * n)(*[g.ids_padded.ctypes.data for g, _, _ in self.items])
+        self._acc = (C.c_void_p * n)(*[g.acc.ctypes.data for g, _, _ in self.items])
+        self._inv = np.ascontiguousarray(np.stack([inv for _, _, inv in self.items]), np.float32).ravel()
+
+    def trace(self, rays: np.ndarray, nthreads: int = 0):
+        """-> (hits dict, instance index per ray, occluded per ray)."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        hits = np.empty((n, 4), np.float32)
+        inst = np.empty(n, np.int32)
+        occ = np.empty(n, np.uint8)
+        lib().orc_trace_instances(len(self.items), C.cast(self._g, C.c_void_p), C.cast(self._off, C.c_void_p),
+                                  C.cast(self._ids, C.c_void_p), C.cast(self._acc, C.c_void_p), self._inv, self.box,
+                                  rays.ravel(), n, hits.ctypes.data, inst.ctypes.data, occ.ctypes.data,
+                                  int(nthreads))
+        return split_hits(hits), inst, occ
 
 
 def grid_params(verts: np.ndarray, ntris: int, k: int) -> dict:

@@ -74,6 +74,23 @@ int main(int argc, char** argv) {
     }
     std::vector<uint8_t> any_batch;
     acc->traceAnyBatch(rv, any_batch);
+    // the scene level: one identity instance of the geometry
+    rtp::InstancedScene scene;
+    scene.buildInstance(std::vector<rt::Instance>{inst});
+    std::vector<rt::Hit> ihits;
+    scene.traceNearestInstance(rv, ihits);
+    if (scene.lastStatus() != RTG_OK) {
+        std::fprintf(stderr, "instance trace failed: %s\n", rtg_last_error());
+        return 1;
+    }
+    std::vector<float> inst_hits(4 * n);
+    for (size_t i = 0; i < n; ++i) {
+        int32_t id = ihits[i].instance ? (int32_t)ihits[i].triangleId : -1;
+        std::memcpy(&inst_hits[4 * i], &id, 4);
+        inst_hits[4 * i + 1] = ihits[i].instance ? ihits[i].distance : 0.f;
+        inst_hits[4 * i + 2] = ihits[i].instance ? ihits[i].v1Coord : 0.f;
+        inst_hits[4 * i + 3] = ihits[i].instance ? ihits[i].v2Coord : 0.f;
+    }
     auto save = [&](const char* suffix, const void* data, size_t bytes) {
         std::string path = std::string(argv[4]) + suffix;
         std::ofstream(path, std::ios::binary).write(static_cast<const char*>(data), (std::streamsize)bytes);
@@ -82,6 +99,7 @@ int main(int argc, char** argv) {
     save(".batch.f32", batch.data(), batch.size() * 4);
     save(".any_single.u8", any_single.data(), any_single.size());
     save(".any_batch.u8", any_batch.data(), any_batch.size());
+    save(".inst.f32", inst_hits.data(), inst_hits.size() * 4);
     rtg_grid_info gi = acc->gridInfo();
     std::printf("{\"res\": [%d, %d, %d], \"nrefs\": %lld}\n", gi.res[0], gi.res[1], gi.res[2], (long long)gi.nrefs);
     return 0;

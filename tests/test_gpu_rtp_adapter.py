@@ -32,6 +32,9 @@ def test_cpp_plugin_mirror(gridlib, oracle, tmp_path):
     single = np.fromfile(p + ".single.f32", np.float32).reshape(-1, 4)
     batch = np.fromfile(p + ".batch.f32", np.float32).reshape(-1, 4)
     assert np.array_equal(single.view(np.uint32), batch.view(np.uint32))
+    # InstancedScene with one identity instance: the same words
+    inst = np.fromfile(p + ".inst.f32", np.float32).reshape(-1, 4)
+    assert np.array_equal(inst.view(np.uint32), batch.view(np.uint32))
     any_s = np.fromfile(p + ".any_single.u8", np.uint8)
     any_b = np.fromfile(p + ".any_batch.u8", np.uint8)
     assert np.array_equal(any_s, any_b)
