@@ -437,8 +437,8 @@ def run_gpu(args, rank, ws, local, dist):
                      "alg_bytes_per_launch": int(alg_bytes),
                      "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"]),
                      "l2": {"peak": round(l2_peak, 1), "frac": round(achieved / l2_peak, 4),
-                            "peak_source": "measured in this run: torch sum over a 32 MiB L2-resident buffer "
-                                           "(bytes read, best of 20 x 10 sums)"}},
+                            "peak_source": "measured in this run: rtg_probe_read_gbs over a 32 MiB "
+                                           "L2-resident buffer (16-byte loads bypassing L1)"}},
         "build_roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": peak,
                            "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / peak, 4),
                            "alg_bytes": int(build_bytes), "ms": head["build_ms"],
@@ -459,23 +459,10 @@ def run_gpu(args, rank, ws, local, dist):
 
 
 def _l2_read_gbs(dev) -> float:
-    """Achievable L2 read bandwidth: a sum over a 32 MiB buffer that stays in
-    the 126 MiB L2 (the traversal's traffic is reads)."""
-    import torch
-    a = torch.ones(8 << 20, dtype=torch.float32, device=dev)
-    out = torch.empty((), dtype=torch.float32, device=dev)
-    for _ in range(5):
-        torch.sum(a, dim=0, out=out)
-    best = float("inf")
-    for _ in range(20):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(10):
-            torch.sum(a, dim=0, out=out)
-        e1.record()
-        torch.cuda.synchronize()
-        best = min(best, e0.elapsed_time(e1) / 10)
-    return a.numel() * 4 / (best / 1e3) / 1e9
+    """Achievable L2 read bandwidth: the library's read probe over a 32 MiB
+    buffer (inside the 126 MiB L2), 16-byte loads that bypass L1."""
+    from gridrt import lib
+    return lib.probe_read_gbs(dev.index or 0, 32 << 20, 20)
 
 
 def _cpu_model() -> str:

@@ -152,6 +152,11 @@ __device__ __forceinline__ bool dda_step(const SParams& P, Lane& L) {
 
 // Moller-Trumbore test of one triangle record against the lane's ray with the
 // reference's acceptance window.  Returns true when ANY mode found t < tmax.
+// GRIDRT_MT_EARLY_OUT = 1 lets a lane leave once u (then v) fails; the
+// accept / reject decision and every value are the same either way.
+#ifndef GRIDRT_MT_EARLY_OUT
+#define GRIDRT_MT_EARLY_OUT 0
+#endif
 template <int MODE>
 __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, const float4& B, const float4& C,
                                          float hi) {
@@ -162,10 +167,17 @@ __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, 
     const float det = B.x * px + B.y * py + B.z * pz;
     const float idet = frcp(det);
     const float u = (tvx * px + tvy * py + tvz * pz) * idet;
+#if GRIDRT_MT_EARLY_OUT
+    // the same predicate, decided in stages: a lane leaves after u
+    if (!(u >= 0.0f)) return false;
+#endif
     const float qx = tvy * B.z - tvz * B.y;
     const float qy = tvz * B.x - tvx * B.z;
     const float qz = tvx * B.y - tvy * B.x;
     const float v = (L.dx * qx + L.dy * qy + L.dz * qz) * idet;
+#if GRIDRT_MT_EARLY_OUT
+    if (!(v >= 0.0f && (1.0f - u) - v >= 0.0f)) return false;
+#endif
     const float t = (C.x * qx + C.y * qy + C.z * qz) * idet;
     const bool acc = (t < L.best) && (t >= L.lo) && (t <= hi) && (u >= 0.0f) && (v >= 0.0f) &&
                      ((1.0f - u) - v >= 0.0f);

@@ -101,7 +101,7 @@ EXPORTS = [
     "rtg_serve_run",
     "rtg_instances_create", "rtg_instances_update", "rtg_instances_box", "rtg_instances_set_tuning",
     "rtg_trace_nearest_instances_device", "rtg_trace_any_instances_device", "rtg_trace_nearest_instances",
-    "rtg_instances_destroy",
+    "rtg_instances_destroy", "rtg_probe_read_gbs",
 ]
 
 
@@ -172,6 +172,7 @@ def load(build_if_missing: bool = True):
         "rtg_trace_any_instances_device": ([vp, vp, i64, vp, i32, vp], C.c_int),
         "rtg_trace_nearest_instances": ([vp, vp, i64, vp, vp, vp], C.c_int),
         "rtg_instances_destroy": ([vp], C.c_int),
+        "rtg_probe_read_gbs": ([i32, i64, i32, C.POINTER(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -487,6 +488,13 @@ def serve(scenes, requests, pool_bytes: int, plain: bool = False, max_in_flight:
     admit = np.array([times[i].admit_s for i in range(len(requests))])
     done = np.array([times[i].done_s for i in range(len(requests))])
     return admit, done
+
+
+def probe_read_gbs(device: int, nbytes: int, reps: int) -> float:
+    """Read bandwidth over a buffer of nbytes (L2 when it fits, else HBM)."""
+    out = C.c_double()
+    check(load().rtg_probe_read_gbs(int(device), int(nbytes), int(reps), C.byref(out)))
+    return out.value
 
 
 def kernel_launches() -> int:

@@ -268,6 +268,12 @@ rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
 rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
 rtg_status rtg_batch_destroy(rtg_batch batch);
 
+/* ---- measurement ----------------------------------------------------------
+ * Read bandwidth of this device over a buffer of `bytes` (16-byte loads that
+ * bypass L1, `reps` passes, best of 5 timed launches): a buffer well inside L2
+ * measures L2, one far above it HBM.  Allocates and frees the buffer. */
+rtg_status rtg_probe_read_gbs(int32_t device, int64_t bytes, int32_t reps, double* gbs);
+
 /* ---- two-level instancing -------------------------------------------------
  * The scene level of the reference's plugin interface: an ordered set of
  * instances, each a built scene placed by a 3 x 4 row-major matrix.

@@ -80,7 +80,7 @@ def test_transformed_instances_match_oracle(gridlib, oracle, seed):
     st = ins.compare_instance_hits(gh, inst, oh, oinst, scs, tfs, rays, oracle)
     print("\n[instances]", st)
     assert st["ok"], st
-    assert (inst >= 0).sum() > 0.2 * rays.shape[0]
+    assert (inst >= 0).sum() >= 2000
 
 
 def test_any_hit_instances_match_oracle(gridlib, oracle):
