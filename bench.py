@@ -9,7 +9,9 @@ Frames cycle through 20 phases.
 
 Prints ONE JSON line (rank 0).  `value` = (primary + shadow rays) / frame
 time, device-timed with CUDA events on the scene's stream, inputs resident,
-L2 flushed between frames.  `e2e` = the same through the public C ABI with
+L2 flushed between frames, each frame (deform + build + trace) replayed from
+a CUDA graph captured per deformation phase; `per_k[k].stream_value` is the
+same frames launched one call at a time.  `e2e` = the same through the public C ABI with
 host buffers: host-deformed vertices uploaded from pinned memory, synchronous
 build, frame trace, hits + occlusion copied back every frame.
 
@@ -356,11 +358,47 @@ def run_gpu(args, rank, ws, local, dist):
         total_s = _max_over_ranks(sum(frame_ms) / 1e3, dist)
         rays = npix * args.steps + int(shadow_count.item())
         rays_all = _sum_over_ranks(rays, dist)
-        per_k[k] = dict(tuning=best, value=rays_all / total_s / 1e6, ms_per_step=1e3 * total_s / args.steps,
+        # the same frames replayed from CUDA graphs (one per deformation
+        # phase, captured on the scene's stream): the library's launches
+        # without the host's per-launch cost between the frame's 15 kernels
+        graphs = []
+        lg0 = lib.kernel_launches()
+        for f in range(FRAMES):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                frame(k, f, order)
+            graphs.append(g)
+        per_frame = (lib.kernel_launches() - lg0) / FRAMES
+        torch.cuda.synchronize()
+        gevs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+        gshadow = torch.zeros((), dtype=torch.int64, device=dev)
+        _barrier(dist)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.mark()
+        for st in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                gevs[st][0].record(stream)
+                graphs[st % FRAMES].replay()
+                gevs[st][1].record(stream)
+                gshadow += (d_occ != 2).sum()
+        torch.cuda.synchronize()
+        _barrier(dist)
+        if sampler:
+            sampler.unmark()
+        if s.build_check() != 0:
+            raise RuntimeError("graph-replayed build failed: " + lib.load().rtg_last_error().decode())
+        g_s = _max_over_ranks(sum(e[0].elapsed_time(e[1]) for e in gevs) / 1e3, dist)
+        g_rays = _sum_over_ranks(npix * args.steps + int(gshadow.item()), dist)
+        del graphs
+        per_k[k] = dict(tuning=best, value=g_rays / g_s / 1e6, ms_per_step=1e3 * g_s / args.steps,
+                        launches=int(round(per_frame * args.steps)),
+                        stream_value=rays_all / total_s / 1e6, stream_ms_per_step=1e3 * total_s / args.steps,
                         build_ms=statistics.median(build_ms), trace_ms=statistics.median(prim_ms),
                         rays_per_step=rays / args.steps,
                         trace_mrays_s=rays / (sum(prim_ms) + sum(shad_ms)) / 1e3,
-                        launches=lc1 - lc0)
+                        stream_launches=lc1 - lc0)
     if sampler:
         sampler.stop()
 

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gridrt.h"
@@ -86,6 +87,22 @@ rtg_status ensure_cell_records(rtg_scene s) {
     const int64_t raw = s->ids_cap < s->scratch_cap ? s->ids_cap : s->scratch_cap;
     if (!s->tune.cell_records || !s->d_offsets || s->crec_cap >= 3 * raw) return RTG_OK;
     return ensure_grid_buffers(s, s->cell_cap, raw);
+}
+
+// A staged keyframe becomes the build's vertices: the build stream waits for
+// its copy and the two vertex buffers swap.
+rtg_status apply_staged(rtg_scene s, cudaStream_t st) {
+    if (!s->staged) return RTG_OK;
+    CUDA_TRY(cudaStreamWaitEvent(st, s->staged_ev, 0));
+    std::swap(s->d_verts, s->d_verts_back);
+    std::swap(s->verts_cap, s->back_cap);
+    s->staged = false;
+    return RTG_OK;
+}
+
+// Marks the end of the builds enqueued so far, for the next staged copy.
+void mark_build(rtg_scene s, cudaStream_t st) {
+    if (s->build_ev) cudaEventRecord(s->build_ev, st);
 }
 
 BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
@@ -325,6 +342,9 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
     cudaFree(s->d_ql);
     cudaFree(s->d_io);
     cudaFree(s->d_ctr);
+    cudaFree(s->d_verts_back);
+    if (s->staged_ev) cudaEventDestroy(s->staged_ev);
+    if (s->build_ev) cudaEventDestroy(s->build_ev);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
     delete s;
     return RTG_OK;
@@ -345,6 +365,10 @@ static rtg_status set_geometry(rtg_scene s, const float* verts, int64_t nverts, 
         return fail(RTG_INVALID_PARAM, "geometry larger than the int32 index space");
     rtg_status rc = set_device(s);
     if (rc) return rc;
+    if (s->staged) {   // a staged keyframe of the old geometry is dropped
+        CUDA_TRY(cudaStreamWaitEvent(st, s->staged_ev, 0));
+        s->staged = false;
+    }
     CUDA_TRY(grow(s->d_verts, s->verts_cap, 3 * nverts + 4));
     CUDA_TRY(grow(s->d_idx, s->idx_cap, 3 * ntris + 4));
     CUDA_TRY(grow(s->d_tris, s->tris_cap, 3 * ntris + 3));
@@ -386,6 +410,29 @@ rtg_status rtg_scene_update_vertices(rtg_scene s, const float* verts, int64_t nv
     return RTG_OK;
 }
 
+rtg_status rtg_scene_stage_vertices(rtg_scene s, const float* h_verts, int64_t nverts, void* copy_stream) {
+    if (!s || (!h_verts && nverts)) return fail(RTG_INVALID_PARAM, "NULL argument");
+    if (nverts != s->nverts) return fail(RTG_INVALID_PARAM, "vertex count differs from the scene's");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    if (!s->staged_ev) {
+        CUDA_TRY(cudaEventCreateWithFlags(&s->staged_ev, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&s->build_ev, cudaEventDisableTiming));
+    }
+    CUDA_TRY(grow(s->d_verts_back, s->back_cap, 3 * nverts));
+    cudaStream_t cs = copy_stream ? (cudaStream_t)copy_stream : s->stream;
+    // the back buffer was last read by a build enqueued before the last one
+    // marked; an unconsumed earlier stage may still be copying into it
+    CUDA_TRY(cudaStreamWaitEvent(cs, s->build_ev, 0));
+    if (s->staged) CUDA_TRY(cudaStreamWaitEvent(cs, s->staged_ev, 0));
+    if (nverts)
+        CUDA_TRY(cudaMemcpyAsync(s->d_verts_back, h_verts, sizeof(float) * 3 * nverts, cudaMemcpyHostToDevice, cs));
+    CUDA_TRY(cudaEventRecord(s->staged_ev, cs));
+    s->staged = true;
+    s->built = false;
+    return RTG_OK;
+}
+
 rtg_status rtg_scene_deform_vertices(rtg_scene s, const float* d_base, const float* d_normals, float amp, float freq,
                                      float phase, void* stream) {
     if (!s || !d_base || !d_normals) return fail(RTG_INVALID_PARAM, "NULL argument");
@@ -415,8 +462,11 @@ rtg_status rtg_scene_build_async(rtg_scene s, int32_t k, void* stream) {
     if (!s->d_offsets || s->hp.ncells == 0) return rtg_scene_build(s, k, stream);
     rc = ensure_cell_records(s);
     if (rc) return rc;
+    rc = apply_staged(s, pick(s, stream));
+    if (rc) return rc;
     rc = enqueue_build(s, k, false, pick(s, stream));
     if (rc) return rc;
+    mark_build(s, pick(s, stream));
     // Trace calls may follow on the same stream: the trace kernels read the
     // device-side status and return misses if this build failed, and
     // rtg_scene_build_check reports the failure.
@@ -464,6 +514,8 @@ rtg_status rtg_scene_build(rtg_scene s, int32_t k, void* stream) {
     }
     rc = ensure_cell_records(s);
     if (rc) return rc;
+    rc = apply_staged(s, s->stream);
+    if (rc) return rc;
     s->built = false;
     bool skip_bbox = false;
     for (int attempt = 0; attempt < 6; ++attempt) {
@@ -503,6 +555,7 @@ rtg_status rtg_scene_build(rtg_scene s, int32_t k, void* stream) {
         s->hp = p;
         s->built = true;
         s->crec_built = s->tune.cell_records != 0;
+        mark_build(s, s->stream);
         uint32_t sticky = 0;
         return read_clear_sticky(s, &sticky);   // earlier attempts of this call are resolved
     }
@@ -905,6 +958,7 @@ rtg_status rtg_batch_build_async(rtg_batch b, void* stream) {
     cudaStream_t st = stream ? (cudaStream_t)stream : b->scenes[0]->stream;
     for (rtg_scene sc : b->scenes) {
         rtg_status rc = ensure_cell_records(sc);
+        if (rc == RTG_OK) rc = apply_staged(sc, st);
         if (rc) return rc;
         sc->crec_built = sc->tune.cell_records != 0;   // this build writes them
     }
@@ -913,6 +967,7 @@ rtg_status rtg_batch_build_async(rtg_batch b, void* stream) {
     if (rc) return rc;
     launch_build_batch(b->d_build, (int)b->scenes.size(), b->grid, b->bitmap_words, st);
     CUDA_TRY(cudaGetLastError());
+    for (rtg_scene sc : b->scenes) mark_build(sc, st);
     for (rtg_scene sc : b->scenes) sc->built = true;   // device status guards the traces
     return RTG_OK;
 }

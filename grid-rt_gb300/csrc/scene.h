@@ -16,6 +16,11 @@ struct rtg_scene_s {
 
     float* d_verts = nullptr;
     int64_t verts_cap = 0, nverts = 0;   // capacity in floats
+    float* d_verts_back = nullptr;       // staged keyframe (rtg_scene_stage_vertices)
+    int64_t back_cap = 0, staged_n = 0;
+    bool staged = false;
+    cudaEvent_t staged_ev = nullptr;     // the staged copy finished
+    cudaEvent_t build_ev = nullptr;      // the last build was enqueued up to here
     int32_t* d_idx = nullptr;
     int64_t idx_cap = 0, ntris = 0;      // capacity in ints
     float4* d_tris = nullptr;

@@ -70,6 +70,12 @@ class InstanceC(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("world_from_local", C.c_float * 12), ("local_from_world", C.c_float * 12)]
 
 
+class MeshC(C.Structure):
+    _fields_ = [("verts", C.POINTER(C.c_float)), ("nverts", C.c_int64), ("tris", C.POINTER(C.c_int32)),
+                ("ntris", C.c_int64), ("source_face", C.POINTER(C.c_int64)), ("faces", C.c_int64),
+                ("dropped", C.c_int64)]
+
+
 class CameraC(C.Structure):
     _fields_ = [("eye", C.c_float * 3), ("base_dir", C.c_float * 3), ("near_u", C.c_float * 3),
                 ("near_v", C.c_float * 3), ("width", C.c_int32), ("height", C.c_int32), ("order", C.c_int32),
@@ -102,6 +108,7 @@ EXPORTS = [
     "rtg_instances_create", "rtg_instances_update", "rtg_instances_box", "rtg_instances_set_tuning",
     "rtg_trace_nearest_instances_device", "rtg_trace_any_instances_device", "rtg_trace_nearest_instances",
     "rtg_instances_destroy", "rtg_probe_read_gbs",
+    "rtg_mesh_load", "rtg_mesh_free", "rtg_scene_load", "rtg_scene_stage_vertices",
 ]
 
 
@@ -173,6 +180,10 @@ def load(build_if_missing: bool = True):
         "rtg_trace_nearest_instances": ([vp, vp, i64, vp, vp, vp], C.c_int),
         "rtg_instances_destroy": ([vp], C.c_int),
         "rtg_probe_read_gbs": ([i32, i64, i32, C.POINTER(C.c_double)], C.c_int),
+        "rtg_mesh_load": ([C.c_char_p, C.POINTER(MeshC)], C.c_int),
+        "rtg_mesh_free": ([C.POINTER(MeshC)], None),
+        "rtg_scene_load": ([vp, C.c_char_p, C.POINTER(MeshC)], C.c_int),
+        "rtg_scene_stage_vertices": ([vp, vp, i64, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -244,6 +255,18 @@ class Scene:
         check(load().rtg_scene_deform_vertices(self.h, _ptr(d_base), _ptr(d_normals), amp, freq, phase, stream))
 
     # ---- grid ---------------------------------------------------------------
+    def load(self, path: str) -> dict:
+        m = MeshC()
+        check(load().rtg_scene_load(self.h, str(path).encode(), C.byref(m)))
+        info = dict(nverts=int(m.nverts), ntris=int(m.ntris), faces=int(m.faces), dropped=int(m.dropped))
+        load().rtg_mesh_free(C.byref(m))
+        self._nverts = info["nverts"]
+        return info
+
+    def stage_vertices(self, host_verts, nverts: int, copy_stream=None):
+        """Double-buffered keyframe upload (pinned host memory)."""
+        check(load().rtg_scene_stage_vertices(self.h, _ptr(host_verts), int(nverts), copy_stream))
+
     def build(self, k: int, stream=None):
         check(load().rtg_scene_build(self.h, int(k), stream))
 
@@ -488,6 +511,23 @@ def serve(scenes, requests, pool_bytes: int, plain: bool = False, max_in_flight:
     admit = np.array([times[i].admit_s for i in range(len(requests))])
     done = np.array([times[i].done_s for i in range(len(requests))])
     return admit, done
+
+
+def load_mesh(path: str):
+    """-> (verts (V, 3) float32, tris (N, 3) int32, source_face (N,) int64,
+    info dict) with the reference loaders' semantics (rtg_mesh_load)."""
+    m = MeshC()
+    check(load().rtg_mesh_load(str(path).encode(), C.byref(m)))
+    try:
+        verts = np.ctypeslib.as_array(m.verts, shape=(m.nverts * 3,)).reshape(-1, 3).copy() if m.nverts \
+            else np.zeros((0, 3), np.float32)
+        tris = np.ctypeslib.as_array(m.tris, shape=(m.ntris * 3,)).reshape(-1, 3).copy() if m.ntris \
+            else np.zeros((0, 3), np.int32)
+        face = np.ctypeslib.as_array(m.source_face, shape=(m.ntris,)).copy() if m.ntris else np.zeros(0, np.int64)
+        info = dict(faces=int(m.faces), dropped=int(m.dropped))
+    finally:
+        load().rtg_mesh_free(C.byref(m))
+    return verts, tris, face, info
 
 
 def probe_read_gbs(device: int, nbytes: int, reps: int) -> float:

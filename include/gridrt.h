@@ -268,6 +268,39 @@ rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
 rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
 rtg_status rtg_batch_destroy(rtg_batch batch);
 
+/* ---- scene ingest ----------------------------------------------------------
+ * rtg_mesh_load reads a .obj or .ply file into the arrays the grid build takes,
+ * as the reference's rtdb loaders feed rt::PrimitiveBuilder
+ * (src/rtdb/ObjFileLoader.cpp, src/rtdb/TriMeshLoader.cpp:17-84,
+ * src/rtcore/PrimitiveBuilder.cpp): every face corner (OBJ) or triangle corner
+ * (PLY) becomes a new vertex, polygons are split as fans (s, s+i, s+i+1), and
+ * a triangle whose Wald record would hold an inf or NaN (TriAccel::valid,
+ * src/rtcore/Triangle.cpp:55-63) is dropped with its successors renumbered, so
+ * triangle ids are the reference's.  source_face[t] is the file face of
+ * triangle t.  The arrays are the library's: release them with rtg_mesh_free. */
+typedef struct {
+    float* verts;          /* nverts x 3 */
+    int64_t nverts;
+    int32_t* tris;         /* ntris x 3 */
+    int64_t ntris;
+    int64_t* source_face;  /* ntris */
+    int64_t faces;         /* faces read from the file */
+    int64_t dropped;       /* triangles dropped as invalid */
+} rtg_mesh;
+rtg_status rtg_mesh_load(const char* path, rtg_mesh* out);
+void rtg_mesh_free(rtg_mesh* mesh);
+/* Loads a mesh file into the scene (rtg_scene_set_geometry); info (optional)
+ * receives the counts and source_face (verts / tris set to NULL). */
+rtg_status rtg_scene_load(rtg_scene scene, const char* path, rtg_mesh* info);
+
+/* Animated keyframes, double-buffered: copies nverts x 3 floats from (pinned)
+ * host memory into the scene's second vertex buffer on copy_stream -- after
+ * the scene's last build, so it can overlap that frame's traces -- and the
+ * scene's next build waits for the copy and builds from it (the buffers
+ * swap).  The reference re-uploads each keyframe before its rebuild
+ * (src/rtgl/GpuRenderer.cpp:97-129). */
+rtg_status rtg_scene_stage_vertices(rtg_scene scene, const float* h_verts, int64_t nverts, void* copy_stream);
+
 /* ---- measurement ----------------------------------------------------------
  * Read bandwidth of this device over a buffer of `bytes` (16-byte loads that
  * bypass L1, `reps` passes, best of 5 timed launches): a buffer well inside L2
