@@ -862,6 +862,103 @@ def run_skewed(args, rank, ws, local, dist):
 
 
 # ---------------------------------------------------------------------------
+# instances: 16 transformed instances of three scenes (two-level trace) and
+# the same world flattened into one scene (one-level trace), 1024^2 camera
+# rays closest hit
+# ---------------------------------------------------------------------------
+def _instance_world(seed: int = 20261203, n_inst: int = 16):
+    rng = np.random.default_rng(seed)
+    base = [scenes.deforming_sphere(0), scenes.plane_and_debris(), scenes.tiny_scene(6, 20_000, spread=1.0)]
+    inst = []
+    for j in range(n_inst):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        sc_ = rng.uniform(0.6, 1.6)
+        t = rng.uniform(-5.0, 5.0, size=3)
+        M = np.concatenate([sc_ * R, t[:, None]], axis=1)
+        Ri = R.T / sc_
+        inv = np.concatenate([Ri, (-Ri @ t)[:, None]], axis=1)
+        inst.append((j % len(base), M.astype(np.float32), inv.astype(np.float32)))
+    return base, inst
+
+
+def run_instances(args, rank, ws, local, dist):
+    import torch
+    from gridrt import lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    base, inst = _instance_world()
+    k = 4
+    scs = []
+    for sc in base:
+        s = lib.Scene(local)
+        s.set_geometry(sc.verts, sc.idx)
+        s.build(k)
+        scs.append(s)
+    I = lib.Instances([(scs[b], M, inv) for b, M, inv in inst])
+    # the flattened world: every instance's vertices taken to world space
+    fv, fi, off = [], [], 0
+    for b, M, _ in inst:
+        v = base[b].verts.astype(np.float64) @ M[:, :3].astype(np.float64).T + M[:, 3].astype(np.float64)
+        fv.append(v.astype(np.float32))
+        fi.append(base[b].idx + off)
+        off += base[b].verts.shape[0]
+    flat = lib.Scene(local)
+    flat.set_geometry(np.concatenate(fv), np.concatenate(fi))
+    flat.build(k)
+    cam = scenes.look_at_camera((11.0, 7.0, 13.0), (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 60.0, WIDTH, HEIGHT)
+    rays = scenes.camera_rays(cam, "morton8")
+    n = rays.shape[0]
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device=dev)
+    d_inst = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(scs[0].stream, device=dev)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            with torch.cuda.stream(stream):
+                fn()
+        torch.cuda.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+        _barrier(dist)
+        for e in evs:
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e[0].record(stream)
+                fn()
+                e[1].record(stream)
+        torch.cuda.synchronize()
+        return _max_over_ranks(sum(e[0].elapsed_time(e[1]) for e in evs) / 1e3, dist)
+
+    t_inst = timed(lambda: I.trace_nearest_device(d_rays, n, d_hits, d_inst, stream=stream.cuda_stream))
+    hit_frac = float((d_inst >= 0).float().mean().item())
+    t_flat = timed(lambda: flat.trace_nearest_device(d_rays, n, d_hits, stream=stream.cuda_stream))
+    rays_all = _sum_over_ranks(n * args.steps, dist)
+    if rank != 0:
+        return
+    tris_inst = sum(base[b].ntris for b, _, _ in inst)
+    print(json.dumps({
+        "metric": "Mrays/s (two-level instanced closest hit)", "value": round(rays_all / t_inst / 1e6, 3),
+        "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t_inst / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "instances_16_of_3_scenes_1024x1024", "k": k, "instances": len(inst),
+                   "scene_triangles": [sc.ntris for sc in base], "instanced_triangles": int(tris_inst),
+                   "hit_fraction": round(hit_frac, 4),
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)"},
+        "flattened": {"value": round(rays_all / t_flat / 1e6, 3), "unit": "Mrays/s",
+                      "ms_per_step": round(1e3 * t_flat / args.steps, 4),
+                      "how": "all instances' triangles taken to world space in one scene, one-level trace"},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # serving: 16 resident scenes, Poisson request streams, continuous batching
 # (rtg_serve_run) versus the plain one-request-at-a-time path
 # ---------------------------------------------------------------------------
@@ -974,7 +1071,8 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
-    ap.add_argument("--workload", default="deforming", choices=["deforming", "batched", "serving", "skewed"])
+    ap.add_argument("--workload", default="deforming",
+                    choices=["deforming", "batched", "serving", "skewed", "instances"])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
     ap.add_argument("--fixed-tuning", default="",
@@ -990,6 +1088,8 @@ def main():
         run_serving(args, rank, ws, local, dist)
     elif args.workload == "skewed":
         run_skewed(args, rank, ws, local, dist)
+    elif args.workload == "instances":
+        run_instances(args, rank, ws, local, dist)
     else:
         run_gpu(args, rank, ws, local, dist)
     if dist is not None:

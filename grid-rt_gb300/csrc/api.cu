@@ -428,8 +428,7 @@ rtg_status rtg_scene_stage_vertices(rtg_scene s, const float* h_verts, int64_t n
     if (nverts)
         CUDA_TRY(cudaMemcpyAsync(s->d_verts_back, h_verts, sizeof(float) * 3 * nverts, cudaMemcpyHostToDevice, cs));
     CUDA_TRY(cudaEventRecord(s->staged_ev, cs));
-    s->staged = true;
-    s->built = false;
+    s->staged = true;   // the current grid stays traceable until the next build
     return RTG_OK;
 }
 
@@ -692,14 +691,17 @@ rtg_status rtg_trace_any(rtg_scene s, const float* rays, int64_t n, uint8_t* occ
     return RTG_OK;
 }
 
-static bool camera_ok(const rtg_camera* cam) {
+}  // extern "C"
+
+namespace gridrt {
+bool camera_ok(const rtg_camera* cam) {
     if (!cam || cam->width <= 0 || cam->height <= 0) return false;
     if ((int64_t)cam->width * cam->height > ((int64_t)1 << 31)) return false;
     if (cam->order == RTG_ORDER_MORTON8 && ((cam->width & 7) || (cam->height & 7))) return false;
     return cam->order == RTG_ORDER_SCANLINE || cam->order == RTG_ORDER_MORTON8;
 }
 
-static CameraArgs camera_args(const rtg_camera* cam) {
+CameraArgs camera_args(const rtg_camera* cam) {
     CameraArgs c;
     for (int a = 0; a < 3; ++a) {
         c.eye[a] = cam->eye[a];
@@ -716,6 +718,9 @@ static CameraArgs camera_args(const rtg_camera* cam) {
     c.order = cam->order;
     return c;
 }
+}  // namespace gridrt
+
+extern "C" {
 
 rtg_status rtg_trace_camera_device(rtg_scene s, const rtg_camera* cam, rtg_hit* d_hits, const float* light_pos,
                                    float* d_shadow_rays, int32_t flags, void* stream) {

@@ -70,4 +70,7 @@ constexpr int32_t kDeferCap = 65536;    // deferred rays a launch can queue; mor
 SceneView scene_view(rtg_scene s);
 // Next per-launch counter slot (and deferred-ray queue) of the scene.
 TraceSlot scene_counter(rtg_scene s);
+// Camera checks and conversion shared by the camera-ray entry points.
+bool camera_ok(const rtg_camera* cam);
+CameraArgs camera_args(const rtg_camera* cam);
 }  // namespace gridrt

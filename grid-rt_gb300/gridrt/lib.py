@@ -70,6 +70,47 @@ class InstanceC(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("world_from_local", C.c_float * 12), ("local_from_world", C.c_float * 12)]
 
 
+class MaterialC(C.Structure):
+    _fields_ = [("type", C.c_int32), ("ambient", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3), ("specular_exponent", C.c_float), ("reflexion", C.c_float),
+                ("refraction_index", C.c_float), ("opacity", C.c_float)]
+
+
+class PointLightC(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("intensity", C.c_float * 3), ("cast_shadows", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class ShadingC(C.Structure):
+    _fields_ = [("d_normals", C.c_void_p), ("d_colors", C.c_void_p), ("d_material", C.c_void_p),
+                ("materials", C.POINTER(MaterialC)), ("nmaterials", C.c_int32),
+                ("lights", C.POINTER(PointLightC)), ("nlights", C.c_int32), ("background", C.c_float * 3),
+                ("max_depth", C.c_int32), ("medium_index", C.c_float)]
+
+
+RTG_MAT_HEADLIGHT, RTG_MAT_HEADLIGHT_COLOR, RTG_MAT_PHONG, RTG_MAT_PHONG_COLOR = 0, 1, 2, 3
+
+
+def material(type=RTG_MAT_PHONG, ambient=(0.2, 0.2, 0.2), diffuse=(1, 1, 1), specular=(1, 1, 1),
+             specular_exponent=32.0, reflexion=0.0, refraction_index=1.0, opacity=1.0) -> MaterialC:
+    """Defaults of PhongMaterial (src/rtplugins/PhongMaterial.cpp:8-17)."""
+    m = MaterialC()
+    m.type = type
+    for a in range(3):
+        m.ambient[a], m.diffuse[a], m.specular[a] = ambient[a], diffuse[a], specular[a]
+    m.specular_exponent, m.reflexion, m.refraction_index, m.opacity = (specular_exponent, reflexion,
+                                                                        refraction_index, opacity)
+    return m
+
+
+def point_light(position, intensity=(1, 1, 1), cast_shadows=True) -> PointLightC:
+    L = PointLightC()
+    for a in range(3):
+        L.position[a], L.intensity[a] = position[a], intensity[a]
+    L.cast_shadows = 1 if cast_shadows else 0
+    return L
+
+
 class MeshC(C.Structure):
     _fields_ = [("verts", C.POINTER(C.c_float)), ("nverts", C.c_int64), ("tris", C.POINTER(C.c_int32)),
                 ("ntris", C.c_int64), ("source_face", C.POINTER(C.c_int64)), ("faces", C.c_int64),
@@ -108,7 +149,7 @@ EXPORTS = [
     "rtg_instances_create", "rtg_instances_update", "rtg_instances_box", "rtg_instances_set_tuning",
     "rtg_trace_nearest_instances_device", "rtg_trace_any_instances_device", "rtg_trace_nearest_instances",
     "rtg_instances_destroy", "rtg_probe_read_gbs",
-    "rtg_mesh_load", "rtg_mesh_free", "rtg_scene_load", "rtg_scene_stage_vertices",
+    "rtg_mesh_load", "rtg_mesh_free", "rtg_scene_load", "rtg_scene_stage_vertices", "rtg_render",
 ]
 
 
@@ -184,6 +225,7 @@ def load(build_if_missing: bool = True):
         "rtg_mesh_free": ([C.POINTER(MeshC)], None),
         "rtg_scene_load": ([vp, C.c_char_p, C.POINTER(MeshC)], C.c_int),
         "rtg_scene_stage_vertices": ([vp, vp, i64, vp], C.c_int),
+        "rtg_render": ([vp, C.POINTER(CameraC), C.POINTER(ShadingC), vp, C.POINTER(C.c_int64), vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -262,6 +304,28 @@ class Scene:
         load().rtg_mesh_free(C.byref(m))
         self._nverts = info["nverts"]
         return info
+
+    def render(self, cam, d_normals, materials, lights, d_rgb, d_colors=None, d_material=None,
+               background=(1.0, 1.0, 1.0), max_depth: int = 3, medium_index: float = 1.0, stream=None) -> int:
+        """Shading wavefront (rtg_render) into d_rgb (H*W*3 float32); returns rays traced."""
+        sh = ShadingC()
+        sh.d_normals = _ptr(d_normals)
+        sh.d_colors = _ptr(d_colors) if d_colors is not None else None
+        sh.d_material = _ptr(d_material) if d_material is not None else None
+        mats = (MaterialC * max(1, len(materials)))(*materials)
+        lts = (PointLightC * max(1, len(lights)))(*lights)
+        sh.materials = mats
+        sh.nmaterials = len(materials)
+        sh.lights = lts
+        sh.nlights = len(lights)
+        for a in range(3):
+            sh.background[a] = background[a]
+        sh.max_depth = max_depth
+        sh.medium_index = medium_index
+        cs = camera_struct(cam, "scanline")
+        rays = C.c_int64()
+        check(load().rtg_render(self.h, C.byref(cs), C.byref(sh), _ptr(d_rgb), C.byref(rays), stream))
+        return rays.value
 
     def stage_vertices(self, host_verts, nverts: int, copy_stream=None):
         """Double-buffered keyframe upload (pinned host memory)."""

@@ -301,6 +301,60 @@ rtg_status rtg_scene_load(rtg_scene scene, const char* path, rtg_mesh* info);
  * (src/rtgl/GpuRenderer.cpp:97-129). */
 rtg_status rtg_scene_stage_vertices(rtg_scene scene, const float* h_verts, int64_t nverts, void* copy_stream);
 
+/* ---- shading wavefront ---------------------------------------------------
+ * rtg_render renders a frame of one scene the way the reference's renderers
+ * call Context::traceNearest per pixel and its materials shade the hit
+ * (src/rtcore/Sample.cpp, src/rtplugins/{HeadlightMaterial,HeadlightMaterialColor,
+ * PhongMaterial,PhongMaterialColor,SimplePointLight,SimpleEnvironment}.cpp), as
+ * a wavefront: primary rays, then per recursion level one closest-hit trace of
+ * every live ray, one any-hit trace of its shadow rays (one per point light),
+ * one shading pass that spawns reflection / refraction rays, and finally the
+ * per-pixel colours combined level by level in the reference's order
+ * (local + reflexion * reflected + (1 - opacity) * refracted).
+ * Shadow rays follow the GPU shader semantics (occluded when a hit lies
+ * before the light); the reference's CPU any-hit is a stub.  Textures are
+ * not applied.  Normals and colours are per vertex (RT_BIND_PER_VERTEX), the
+ * material per triangle.  Synchronous: returns when d_rgb is written. */
+enum {
+    RTG_MAT_HEADLIGHT = 0,        /* vertex colours */
+    RTG_MAT_HEADLIGHT_COLOR = 1,  /* material diffuse colour */
+    RTG_MAT_PHONG = 2,            /* vertex colours */
+    RTG_MAT_PHONG_COLOR = 3       /* material diffuse colour */
+};
+typedef struct {
+    int32_t type;
+    float ambient[3];
+    float diffuse[3];
+    float specular[3];
+    float specular_exponent;
+    float reflexion;              /* PhongMaterial::setReflexCoeff */
+    float refraction_index;
+    float opacity;
+} rtg_material;
+typedef struct {
+    float position[3];
+    float intensity[3];
+    int32_t cast_shadows;
+    int32_t pad;
+} rtg_point_light;
+typedef struct {
+    const float* d_normals;       /* nverts x 3 (device) */
+    const float* d_colors;        /* nverts x 3 (device), NULL: white */
+    const int32_t* d_material;    /* ntris material indices (device), NULL: material 0 */
+    const rtg_material* materials;   /* host */
+    int32_t nmaterials;
+    const rtg_point_light* lights;   /* host */
+    int32_t nlights;
+    float background[3];          /* SimpleEnvironment */
+    int32_t max_depth;            /* Context::setMaxRecursionDepth (default 3) */
+    float medium_index;           /* Context::setMediumRefractionIndex (default 1) */
+} rtg_shading;
+/* d_rgb: width x height x 3 float32, row-major from the bottom row (the
+ * camera's pixel order, scanline).  rays_out (optional): rays traced in total
+ * (primary, shadow, reflected, refracted). */
+rtg_status rtg_render(rtg_scene scene, const rtg_camera* cam, const rtg_shading* shading, float* d_rgb,
+                      int64_t* rays_out, void* stream);
+
 /* ---- measurement ----------------------------------------------------------
  * Read bandwidth of this device over a buffer of `bytes` (16-byte loads that
  * bypass L1, `reps` passes, best of 5 timed launches): a buffer well inside L2

@@ -560,3 +560,144 @@ void orc_trace_instances(int32_t ninst, const orc_grid_info* const* g, const int
         if (inst_out) inst_out[i] = found;
     }
 }
+
+/* ---- shading: the reference's per-pixel recursion ------------------------
+ * Context::traceNearest + material / environment shade
+ * (src/rtcore/Sample.cpp, src/rtplugins/{HeadlightMaterial,HeadlightMaterialColor,
+ * PhongMaterial,PhongMaterialColor,SimplePointLight,SimpleEnvironment}.cpp).
+ * Shadow rays are occluded when the closest hit before the light has
+ * t < 1 (the GPU shader semantics; the CPU any-hit is a stub).  vr::vec3f is
+ * absent from the checkout: normalise = v * (1 / sqrt(v.v)). */
+typedef struct { float x, y, z; } ov3;
+static inline ov3 o3(float x, float y, float z) { ov3 r = {x, y, z}; return r; }
+static inline ov3 oadd(ov3 a, ov3 b) { return o3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline ov3 osub(ov3 a, ov3 b) { return o3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline ov3 osc(ov3 a, float s) { return o3(a.x * s, a.y * s, a.z * s); }
+static inline ov3 omul(ov3 a, ov3 b) { return o3(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline float odot(ov3 a, ov3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline ov3 onorm(ov3 a) { float inv = 1.0f / sqrtf(odot(a, a)); return osc(a, inv); }
+static inline ov3 orefl(ov3 i, ov3 n) { return osub(i, osc(n, odot(i, n) * 2.0f)); }
+
+typedef struct {
+    const orc_grid_info* g; const int32_t* offsets; const int32_t* ids; const float* acc;
+    const int32_t* idx; const float* normals; const float* colors; const int32_t* material;
+    const orc_material* mats; int32_t nmats; const orc_light* lights; int32_t nlights;
+    const float* bg; int32_t max_depth; float medium;
+} shade_ctx;
+
+static int closest(const shade_ctx* C, ov3 o, ov3 d, float tnear, float tfar, ohit* h, float* t) {
+    oray r;
+    r.orig[0] = o.x; r.orig[1] = o.y; r.orig[2] = o.z;
+    r.dir[0] = d.x; r.dir[1] = d.y; r.dir[2] = d.z;
+    r.tnear = tnear;
+    r.tfar = tfar;
+    ray_update(&r);
+    h->id = -1;
+    return C->g->ncells > 0 && trace_one(C->g, C->offsets, C->ids, C->acc, &r, h, t, NULL, NULL);
+}
+
+static ov3 shade_ray(const shade_ctx* C, ov3 o, ov3 d, int depth, int64_t* nrays) {
+    ohit h;
+    float t = 0.f;
+    ++*nrays;
+    if (!closest(C, o, d, 2e-4f, FLT_MAX, &h, &t)) return o3(C->bg[0], C->bg[1], C->bg[2]);
+    const int64_t tri = h.id;
+    const float b[3] = {1.0f - h.u - h.v, h.u, h.v};
+    ov3 n = o3(0.f, 0.f, 0.f), vc = o3(0.f, 0.f, 0.f);
+    for (int k = 0; k < 3; ++k) {
+        const float* nk = C->normals + 3 * (int64_t)C->idx[3 * tri + k];
+        n = oadd(n, osc(o3(nk[0], nk[1], nk[2]), b[k]));
+        if (C->colors) {
+            const float* ck = C->colors + 3 * (int64_t)C->idx[3 * tri + k];
+            vc = oadd(vc, osc(o3(ck[0], ck[1], ck[2]), b[k]));
+        }
+    }
+    if (!C->colors) vc = o3(1.f, 1.f, 1.f);
+    n = onorm(n);
+    const int m = C->material ? C->material[tri] : 0;
+    orc_material M;
+    memset(&M, 0, sizeof(M));
+    if (m >= 0 && m < C->nmats) M = C->mats[m];
+    else { M.type = 0; M.ambient[0] = M.ambient[1] = M.ambient[2] = 0.1f; }
+    const ov3 amb = o3(M.ambient[0], M.ambient[1], M.ambient[2]);
+    if (M.type == 0 || M.type == 1) {   /* headlight */
+        const ov3 c = M.type == 0 ? vc : o3(M.diffuse[0], M.diffuse[1], M.diffuse[2]);
+        const float ndd = -odot(n, onorm(d));
+        return omul(oadd(amb, osc(osub(c, amb), ndd)), c);
+    }
+    const ov3 p = oadd(o, osc(d, t));
+    const ov3 spec = onorm(orefl(d, n));
+    const ov3 hp = oadd(p, osc(n, 2e-4f));
+    ov3 dif = o3(0.f, 0.f, 0.f), spc = o3(0.f, 0.f, 0.f);
+    for (int i = 0; i < C->nlights; ++i) {
+        const orc_light* Lt = &C->lights[i];
+        if (odot(n, d) > 0.0f) continue;                      /* back face */
+        const ov3 L = osub(o3(Lt->position[0], Lt->position[1], Lt->position[2]), hp);
+        if (odot(n, L) <= 0.0f) continue;                     /* initShadowRay */
+        if (Lt->cast_shadows) {
+            ohit sh;
+            float st = 0.f;
+            ++*nrays;
+            if (closest(C, hp, L, 2e-4f, 1.0f, &sh, &st) && st < 1.0f) continue;
+        }
+        const ov3 Ld = onorm(L);
+        const ov3 lc = o3(Lt->intensity[0], Lt->intensity[1], Lt->intensity[2]);
+        dif = oadd(dif, osc(lc, odot(n, Ld)));
+        if (M.type == 2 || M.specular_exponent > 0.0f) {
+            const float sdl = odot(spec, Ld);
+            if (sdl > 0.0f) spc = oadd(spc, osc(lc, powf(sdl, M.specular_exponent)));
+        }
+    }
+    const ov3 sc = o3(M.specular[0], M.specular[1], M.specular[2]);
+    ov3 out;
+    if (M.type == 2) {
+        out = oadd(omul(vc, oadd(amb, dif)), omul(sc, spc));
+    } else {
+        out = omul(o3(M.diffuse[0], M.diffuse[1], M.diffuse[2]), dif);
+        out = oadd(out, oadd(amb, omul(sc, spc)));
+    }
+    if (depth >= C->max_depth) return out;
+    if (M.reflexion > 0.0f) {
+        const ov3 rc = shade_ray(C, p, orefl(d, n), depth + 1, nrays);
+        out = oadd(out, osc(rc, M.reflexion));
+    }
+    if (M.opacity < 1.0f) {
+        const int front = odot(n, d) <= 0.0f;
+        const ov3 nn = front ? n : osc(n, -1.0f);
+        const float ratio = front ? C->medium / M.refraction_index : M.refraction_index / C->medium;
+        const ov3 nd = onorm(d);
+        const float cosI = -odot(nn, nd);
+        const float cosT2 = 1.0f - ratio * ratio * (1.0f - cosI * cosI);
+        if (cosT2 > 0.0f) {
+            const float cosT = sqrtf(cosT2);
+            const ov3 td = oadd(osc(nd, ratio), osc(nn, ratio * cosI - cosT));
+            const ov3 rc = shade_ray(C, p, td, depth + 1, nrays);
+            out = oadd(out, osc(rc, 1.0f - M.opacity));
+        }
+    }
+    return out;
+}
+
+int64_t orc_render(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc,
+                   const int32_t* idx, const float* normals, const float* colors, const int32_t* material,
+                   const orc_material* mats, int32_t nmats, const orc_light* lights, int32_t nlights,
+                   const float* background, int32_t max_depth, float medium, const float* primary, int64_t n,
+                   float* rgb, int nthreads) {
+    shade_ctx C = {g, offsets, ids, acc, idx, normals, colors, material, mats, nmats, lights, nlights,
+                   background, max_depth, medium};
+    int64_t total = 0;
+#ifdef _OPENMP
+    int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt) reduction(+ : total)
+#endif
+    for (int64_t i = 0; i < n; ++i) {
+        const float* q = primary + 8 * i;
+        int64_t nr = 0;
+        const ov3 c = shade_ray(&C, o3(q[0], q[1], q[2]), o3(q[4], q[5], q[6]), 0, &nr);
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+        total += nr;
+    }
+    return total;
+}

@@ -76,6 +76,24 @@ void orc_trace_instances(int32_t ninst, const orc_grid_info* const* g, const int
                          const float* rays, int64_t n, float* hits, int32_t* inst_out, uint8_t* occluded,
                          int nthreads);
 
+/* Shading (see oracle.c): materials and point lights with the layout of the
+ * library's rtg_material / rtg_point_light; primary rays n x 8; rgb n x 3.
+ * Returns the rays traced (primary, shadow, reflected, refracted). */
+typedef struct {
+    int32_t type;   /* 0 headlight, 1 headlight colour, 2 phong, 3 phong colour */
+    float ambient[3], diffuse[3], specular[3];
+    float specular_exponent, reflexion, refraction_index, opacity;
+} orc_material;
+typedef struct {
+    float position[3], intensity[3];
+    int32_t cast_shadows, pad;
+} orc_light;
+int64_t orc_render(const orc_grid_info* g, const int32_t* offsets, const int32_t* ids, const float* acc,
+                   const int32_t* idx, const float* normals, const float* colors, const int32_t* material,
+                   const orc_material* mats, int32_t nmats, const orc_light* lights, int32_t nlights,
+                   const float* background, int32_t max_depth, float medium, const float* primary, int64_t n,
+                   float* rgb, int nthreads);
+
 /* Number of OpenMP threads the trace entry points use when nthreads <= 0. */
 int orc_max_threads(void);
 

@@ -126,6 +126,42 @@ class Grid:
         return (occ, cnt) if counters else occ
 
 
+class Material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("ambient", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3), ("specular_exponent", C.c_float), ("reflexion", C.c_float),
+                ("refraction_index", C.c_float), ("opacity", C.c_float)]
+
+
+class Light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("intensity", C.c_float * 3), ("cast_shadows", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+def render(grid: "Grid", normals, colors, material, mats, lights, background, max_depth, medium, primary,
+           nthreads: int = 0):
+    """Restated per-pixel shading recursion -> (rgb (n, 3) float32, rays traced)."""
+    primary = np.ascontiguousarray(primary, np.float32).reshape(-1, 8)
+    n = primary.shape[0]
+    rgb = np.empty((n, 3), np.float32)
+    normals = np.ascontiguousarray(normals, np.float32)
+    colors = None if colors is None else np.ascontiguousarray(colors, np.float32)
+    material = None if material is None else np.ascontiguousarray(material, np.int32)
+    M = (Material * max(1, len(mats)))(*mats)
+    Lt = (Light * max(1, len(lights)))(*lights)
+    bg = np.ascontiguousarray(background, np.float32)
+    L = lib()
+    L.orc_render.restype = C.c_int64
+    L.orc_render.argtypes = [C.POINTER(GridInfo), _i32p, _i32p, _f32p, _i32p, _f32p, C.c_void_p, C.c_void_p,
+                             C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, _f32p, C.c_int32, C.c_float, _f32p,
+                             C.c_int64, _f32p, C.c_int]
+    total = L.orc_render(C.byref(grid.info), grid.offsets, grid.ids_padded, grid.acc.ravel(), grid.idx.ravel(),
+                         normals.ravel(), None if colors is None else colors.ctypes.data,
+                         None if material is None else material.ctypes.data, C.cast(M, C.c_void_p), len(mats),
+                         C.cast(Lt, C.c_void_p), len(lights), bg, int(max_depth), float(medium), primary.ravel(), n,
+                         rgb.ravel(), int(nthreads))
+    return rgb, int(total)
+
+
 class Instances:
     """Oracle instance set: (Grid, world_from_local 3x4, local_from_world 3x4)
     triples, restating Context::instantiateGeometry, buildInstance and
