@@ -157,6 +157,12 @@ __device__ __forceinline__ bool dda_step(const SParams& P, Lane& L) {
 #ifndef GRIDRT_MT_EARLY_OUT
 #define GRIDRT_MT_EARLY_OUT 0
 #endif
+// GRIDRT_MT_FAST_RCP = 1 takes 1/det from the hardware's approximate
+// reciprocal instead of the correctly rounded one (decisions move only at
+// near-ties: a relative error of about 2^-23 in u, v, t).
+#ifndef GRIDRT_MT_FAST_RCP
+#define GRIDRT_MT_FAST_RCP 0
+#endif
 template <int MODE>
 __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, const float4& B, const float4& C,
                                          float hi) {
@@ -165,7 +171,12 @@ __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, 
     const float py = L.dz * C.x - L.dx * C.z;
     const float pz = L.dx * C.y - L.dy * C.x;
     const float det = B.x * px + B.y * py + B.z * pz;
+#if GRIDRT_MT_FAST_RCP
+    float idet;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(idet) : "f"(det));
+#else
     const float idet = frcp(det);
+#endif
     const float u = (tvx * px + tvy * py + tvz * pz) * idet;
 #if GRIDRT_MT_EARLY_OUT
     // the same predicate, decided in stages: a lane leaves after u
