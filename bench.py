@@ -959,6 +959,71 @@ def run_instances(args, rank, ws, local, dist):
 
 
 # ---------------------------------------------------------------------------
+# render: the shading wavefront (rtg_render) on the plane-and-debris scene,
+# 1024^2 pixels, Phong / headlight materials, two point lights (one casting
+# shadows), reflection on the plane, refraction on a quarter of the debris,
+# recursion depth 3
+# ---------------------------------------------------------------------------
+def run_render(args, rank, ws, local, dist):
+    import torch
+    from gridrt import lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc = scenes.plane_and_debris()
+    s = lib.Scene(local)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(4)
+    v = sc.verts.astype(np.float64)
+    f = sc.idx
+    fn = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    nrm = np.zeros_like(v)
+    for kk in range(3):
+        np.add.at(nrm, f[:, kk], fn)
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-30)
+    rng = np.random.default_rng(20261207)
+    colors = rng.uniform(0.2, 1.0, size=sc.verts.shape).astype(np.float32)
+    mat = (np.arange(sc.ntris) % 4).astype(np.int32)
+    mat[:32768] = 0
+    mats = [lib.material(lib.RTG_MAT_PHONG, reflexion=0.35),
+            lib.material(lib.RTG_MAT_PHONG_COLOR, diffuse=(0.8, 0.3, 0.2), opacity=0.6, refraction_index=1.3),
+            lib.material(lib.RTG_MAT_HEADLIGHT, ambient=(0.1, 0.1, 0.1)),
+            lib.material(lib.RTG_MAT_HEADLIGHT_COLOR, ambient=(0.1, 0.1, 0.1), diffuse=(0.2, 0.6, 0.9))]
+    lights = [lib.point_light((2.0, 4.0, 2.0), (0.8, 0.8, 0.8), True),
+              lib.point_light((-3.0, 2.0, 1.0), (0.3, 0.3, 0.4), False)]
+    d_n = torch.from_numpy(nrm.astype(np.float32)).to(dev)
+    d_c = torch.from_numpy(colors).to(dev)
+    d_m = torch.from_numpy(mat).to(dev)
+    cam = scenes.plane_and_debris_camera(WIDTH, HEIGHT)
+    d_rgb = torch.empty((WIDTH * HEIGHT, 3), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        s.render(cam, d_n, mats, lights, d_rgb, d_colors=d_c, d_material=d_m, max_depth=3)
+    torch.cuda.synchronize()
+    _barrier(dist)
+    total, rays = 0.0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rays += s.render(cam, d_n, mats, lights, d_rgb, d_colors=d_c, d_material=d_m, max_depth=3)
+        total += time.perf_counter() - t0
+    total = _max_over_ranks(total, dist)
+    rays_all = _sum_over_ranks(rays, dist)
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "Mrays/s (shading wavefront: primary + shadow + reflected + refracted)",
+        "value": round(rays_all / total / 1e6, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "render_plane_and_debris_1024x1024_depth3", "k": 4, "rays_per_step": rays // args.steps,
+                   "timing": "host clock around the synchronous rtg_render call (per-level count read-backs "
+                             "included); L2 flushed before each frame, outside the timed call"},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------------------
 # serving: 16 resident scenes, Poisson request streams, continuous batching
 # (rtg_serve_run) versus the plain one-request-at-a-time path
 # ---------------------------------------------------------------------------
@@ -1072,7 +1137,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
     ap.add_argument("--workload", default="deforming",
-                    choices=["deforming", "batched", "serving", "skewed", "instances"])
+                    choices=["deforming", "batched", "serving", "skewed", "instances", "render"])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
     ap.add_argument("--fixed-tuning", default="",
@@ -1090,6 +1155,8 @@ def main():
         run_skewed(args, rank, ws, local, dist)
     elif args.workload == "instances":
         run_instances(args, rank, ws, local, dist)
+    elif args.workload == "render":
+        run_render(args, rank, ws, local, dist)
     else:
         run_gpu(args, rank, ws, local, dist)
     if dist is not None:
