@@ -1074,8 +1074,12 @@ def run_serving(args, rank, ws, local, dist):
             reqs.append((arr, si, mode, src.data_ptr() + 32 * off, n, h_out))
         return reqs
 
-    def run(reqs, plain):
-        admit, done = lib.serve(scs, reqs, pool_bytes=pool_bytes, plain=plain, max_in_flight=3)
+    def run(reqs, plain, in_flight=None):
+        # plain = one request at a time: upload, single-scene trace, download, wait
+        # (in_flight 1); plain_pipelined keeps three such requests in flight
+        if in_flight is None:
+            in_flight = 1 if plain else 3
+        admit, done = lib.serve(scs, reqs, pool_bytes=pool_bytes, plain=plain, max_in_flight=in_flight)
         arr = np.array([q[0] for q in reqs])
         lat = done - arr
         rays = sum(q[4] for q in reqs)
@@ -1095,7 +1099,8 @@ def run_serving(args, rank, ws, local, dist):
         reqs = make_requests(rate, count, 100 + rate)
         out[str(rate)] = {"served": run(reqs, False), "plain": run(reqs, True)}
     sat = make_requests(None, args.serve_saturation, 7)
-    saturation = {"served": run(sat, False), "plain": run(sat, True)}
+    saturation = {"served": run(sat, False), "plain": run(sat, True),
+                  "plain_pipelined": run(sat, True, in_flight=3)}
     if rank != 0:
         return
     print(json.dumps({
@@ -1105,9 +1110,11 @@ def run_serving(args, rank, ws, local, dist):
         "config": {"workload": "serving_16_scenes", "scenes": nscenes, "triangles": tris,
                    "scene_bytes": int(scene_bytes), "pool_bytes": pool_bytes, "hbm_budget_bytes": budget,
                    "rays_per_request": "log-uniform [1e3, 4e6]", "modes": "70% closest / 30% any-hit",
-                   "max_in_flight": 3},
+                   "max_in_flight": {"served": 3, "plain": 1, "plain_pipelined": 3}},
         "saturation": saturation, "served_over_plain": round(saturation["served"]["mrays_s"] /
                                                               saturation["plain"]["mrays_s"], 3),
+        "served_over_plain_pipelined": round(saturation["served"]["mrays_s"] /
+                                             saturation["plain_pipelined"]["mrays_s"], 3),
         "rates": out,
     }), flush=True)
 

@@ -683,17 +683,14 @@ __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offs
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
-    // a warp takes 32 queued cells: each lane sorts its own cell when it has
-    // at most 8 entries (19-comparator network in registers); the larger
-    // ones (9..32) are then sorted one after another by the whole warp
-    for (int64_t base = warp * 32; base < nq; base += nwarps * 32) {
-        const int64_t i = base + lane;
-        int32_t s = 0, n = 0;
-        if (i < nq) {
-            const int32_t c = q[i];
-            s = offsets[c];
-            n = offsets[c + 1] - s;
-        }
+    // cells of at most 8 entries: one per thread, a 19-comparator network in
+    // registers; then cells of 9..32 entries: one per warp, a bitonic
+    // network over the lanes
+    const int64_t tid = (int64_t)vbx * blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)vgx * blockDim.x;
+    for (int64_t i = tid; i < nq; i += nthreads) {
+        const int32_t c = q[i];
+        const int32_t s = offsets[c], n = offsets[c + 1] - s;
         if (n <= 8) {
             int32_t v[8];
 #pragma unroll
@@ -710,11 +707,11 @@ __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offs
             for (int k = 0; k < 8; ++k)
                 if (k < n) ids[s + k] = v[k];
         }
-        unsigned big = __ballot_sync(FULL, n > 8);
-        while (big) {
-            const int src = __ffs(big) - 1;
-            big &= big - 1;
-            const int32_t cs = __shfl_sync(FULL, s, src), cn = __shfl_sync(FULL, n, src);
+    }
+    for (int64_t i = warp; i < nq; i += nwarps) {
+        const int32_t c = q[i];
+        const int32_t cs = offsets[c], cn = offsets[c + 1] - cs;
+        if (cn > 8) {
             int32_t v = lane < cn ? ids[cs + lane] : INT_MAX;
 #pragma unroll
             for (int k = 2; k <= 32; k <<= 1) {
@@ -954,7 +951,7 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     out[BK_TRI] = clampi((a.ntris + 255) / 256, 16 * sms);            // one warp per 32 triangles
     out[BK_TILE] = clampi((a.cell_cap + SCAN_TILE - 1) / SCAN_TILE, 8 * sms);
     out[BK_ONE] = 1;
-    out[BK_SSMALL] = clampi(a.cell_cap / 4096 + 1, 8 * sms);            // 32 cells a warp
+    out[BK_SSMALL] = clampi(a.cell_cap / 512 + 1, 8 * sms);
     out[BK_SMED] = clampi(a.cell_cap / 2048 + 1, 4 * sms);             // 16 warps a block, one cell a warp
     out[BK_SLARGE] = clampi(a.cell_cap / 16384 + 1, 2 * sms);
     out[BK_REFS] = a.crec ? clampi((a.ref_cap + 255) / 256, 16 * sms) : 0;
