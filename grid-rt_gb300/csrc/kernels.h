@@ -86,7 +86,7 @@ struct TraceTuning {
     int persistent = 1;    // 1: persistent warps over ray batches; 0: one batch per warp
     int cell_records = 0;  // 1: the build also writes triangle records in cell-list order
     int heavy_cell = 32;   // > 0: rays meeting a list longer than this finish in a warp-per-ray pass
-    int heavy_lanes = 8;   // lanes per deferred ray in that pass: 4, 8, 16 or 32
+    int heavy_lanes = 32;  // lanes per deferred ray in that pass: 4, 8, 16 or 32
 };
 
 // Per-launch device state of a single-scene trace: three counters the launch

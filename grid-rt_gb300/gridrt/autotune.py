@@ -25,8 +25,8 @@ SPACE = {
     "order": ("scanline", "morton8"),
     "empty_run": (2, 4, 8),
     "persistent": (True, False),
-    "heavy_cell": (0, 16, 32, 64),
-    "heavy_lanes": (4, 8, 16, 32),
+    "heavy_cell": (0, 32, 48),
+    "heavy_lanes": (16, 32),
     "cell_records": (False, True),
 }
 

@@ -446,7 +446,7 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *                        second pass that traces it with a group of lanes (the list split
  *                        over them); default 32, 0 off.  Results are identical either way.
  *                        Costs 16 MB of device memory per scene (deferred-ray queues).
- *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8 (default), 16, 32 */
+ *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8, 16, 32 (default) */
 enum {
     RTG_TUNE_EMPTY_RUN = 1,
     RTG_TUNE_PERSISTENT = 2,
