@@ -542,6 +542,17 @@ __device__ __forceinline__ void flush_counters(TraceCounters* ctr, uint32_t star
 #define GRIDRT_TRACE_MIN_BLOCKS 8
 #endif
 
+// GRIDRT_REFILL = 1: instead of tracing a claimed batch of 32 rays to its
+// end, the warp hands new rays to its idle lanes whenever at least
+// GRIDRT_REFILL_MIN of them are idle (one claim for all of them), keeping the
+// lanes busy while a batch's long rays finish.
+#ifndef GRIDRT_REFILL
+#define GRIDRT_REFILL 0
+#endif
+#ifndef GRIDRT_REFILL_MIN
+#define GRIDRT_REFILL_MIN 16
+#endif
+
 template <int MODE, bool COUNT, int ER>
 __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(SceneView s, TraceIO io) {
     __shared__ SParams P;
@@ -549,6 +560,69 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(Sce
     const int lane = threadIdx.x & 31;
     Lane L;
     uint32_t cells = 0, tests = 0, started = 0;
+#if GRIDRT_REFILL
+    bool active = false, exhausted = false;
+    int32_t heavy = io.heavy, work_cap = kNoHeavy;
+    for (;;) {
+        const unsigned idle = __ballot_sync(FULL, !active);
+        if (!exhausted && (__popc(idle) >= GRIDRT_REFILL_MIN || idle == FULL)) {
+            const unsigned need = (unsigned)__popc(idle);
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(io.counter, (unsigned long long)need);
+            b = __shfl_sync(FULL, b, 0);
+            if ((long long)(b + need) >= io.n) exhausted = true;
+            if (!active) {
+                const long long ray = (long long)b + __popc(idle & ((1u << lane) - 1u));
+                if (ray < io.n) {
+                    L.ray = (int32_t)ray;
+                    heavy = io.heavy;
+                    work_cap = heavy < kNoHeavy / (kHeavyWorkMult + 1) && kHeavyWorkMult > 0 ? heavy * kHeavyWorkMult
+                                                                                             : kNoHeavy;
+                    ++started;
+                    if (start_ray<MODE>(P, io, L, L.ray)) {
+                        active = true;
+                    } else {
+                        if (L.id != -2) L.id = -1;
+                        finish_ray<MODE>(io, P, s.tris, L);
+                    }
+                }
+            }
+        }
+        if (!__any_sync(FULL, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        bool fin = active &&
+                   advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, s.crec, heavy, work_cap, cells, tests);
+        if (io.defer) {
+            const bool d = fin && L.id == kDeferred;
+            const unsigned m = __ballot_sync(FULL, d);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                unsigned long long at = 0;
+                if (lane == leader) at = atomicAdd(io.counter + 1, (unsigned long long)__popc(m));
+                at = __shfl_sync(FULL, at, leader);
+                if (d) {
+                    const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
+                    if (slot < (unsigned long long)io.defer_cap) {
+                        io.defer[slot] = make_int2(L.ray + io.defer_base,
+                                                   L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
+                        active = false;
+                    } else {
+                        heavy = kNoHeavy;
+                        work_cap = kNoHeavy;
+                        L.id = -1;
+                    }
+                    fin = false;
+                }
+            }
+        }
+        if (fin) {
+            finish_ray<MODE>(io, P, s.tris, L);
+            active = false;
+        }
+    }
+#else
     for (;;) {
         // the warp claims the next 32 consecutive rays and traces them to the end
         unsigned long long b = 0;
@@ -557,6 +631,7 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(Sce
         if ((long long)b >= io.n) break;
         trace_batch32<MODE, ER>(P, s, io, L, (long long)b, cells, tests, started);
     }
+#endif
     if (COUNT) flush_counters(io.ctr, started, cells, tests);
 }
 
