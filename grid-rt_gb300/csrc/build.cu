@@ -160,6 +160,7 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
 template <bool MULTI>
 __global__ void __launch_bounds__(256) bbox_params_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -197,6 +198,7 @@ __device__ __forceinline__ void zero_offsets_body(int32_t* __restrict__ offsets,
 template <bool MULTI>
 __global__ void zero_offsets_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -335,6 +337,7 @@ __device__ __forceinline__ void count_body(const float* __restrict__ verts, cons
 template <bool MULTI>
 __global__ void __launch_bounds__(256) count_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -416,6 +419,7 @@ __device__ __forceinline__ void scatter_body(const float* __restrict__ verts, co
 template <bool MULTI>
 __global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -470,6 +474,7 @@ __device__ __forceinline__ void scan_reduce_body(const int32_t* __restrict__ cou
 template <bool MULTI>
 __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -527,6 +532,7 @@ __device__ __forceinline__ void scan_tiles_body(GridParams* p, BuildWork* w, int
 template <bool MULTI>
 __global__ void __launch_bounds__(1024) scan_tiles_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -658,6 +664,7 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
 template <bool MULTI>
 __global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -731,6 +738,7 @@ __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offs
 template <bool MULTI>
 __global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -783,6 +791,7 @@ __device__ __forceinline__ void sort_medium_body(const int32_t* __restrict__ off
 template <bool MULTI>
 __global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -901,6 +910,7 @@ __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offs
 template <bool MULTI>
 __global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
                        int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -929,6 +939,7 @@ __device__ __forceinline__ void cell_records_body(const int32_t* __restrict__ id
 template <bool MULTI>
 __global__ void __launch_bounds__(256) cell_records_kernel(BuildArgs one, const BuildArgs* __restrict__ many,
                                                            const int* __restrict__ first, int ntasks) {
+    pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
@@ -963,20 +974,21 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     count_launches(skip_bbox ? 9 : 10);
     const int* f[kBuildKinds];
     for (int k = 0; k < kBuildKinds; ++k) f[k] = MULTI ? g.first[k] : nullptr;
-    if (!skip_bbox) bbox_params_kernel<MULTI><<<g.total[BK_BBOX], 256, 0, st>>>(one, many, f[BK_BBOX], ntasks);
-    zero_offsets_kernel<MULTI><<<g.total[BK_ZERO], 256, 0, st>>>(one, many, f[BK_ZERO], ntasks);
-    count_kernel<MULTI><<<g.total[BK_TRI], 256, 0, st>>>(one, many, f[BK_TRI], ntasks);
-    scan_reduce_kernel<MULTI><<<g.total[BK_TILE], SCAN_THREADS, 0, st>>>(one, many, f[BK_TILE], ntasks);
-    scan_tiles_kernel<MULTI><<<g.total[BK_ONE], 1024, 0, st>>>(one, many, f[BK_ONE], ntasks);
-    scan_down_kernel<MULTI><<<g.total[BK_TILE], SCAN_THREADS, 0, st>>>(one, many, f[BK_TILE], ntasks);
-    scatter_kernel<MULTI><<<g.total[BK_TRI], 256, 0, st>>>(one, many, f[BK_TRI], ntasks);
-    sort_small_kernel<MULTI><<<g.total[BK_SSMALL], 256, 0, st>>>(one, many, f[BK_SSMALL], ntasks);
-    sort_medium_kernel<MULTI><<<g.total[BK_SMED], 512, 0, st>>>(one, many, f[BK_SMED], ntasks);
-    sort_large_kernel<MULTI><<<g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, st>>>(one, many, f[BK_SLARGE],
-                                                                                         ntasks);
+    if (!skip_bbox)
+        launch_k(bbox_params_kernel<MULTI>, g.total[BK_BBOX], 256, 0, st, one, many, f[BK_BBOX], ntasks);
+    launch_k(zero_offsets_kernel<MULTI>, g.total[BK_ZERO], 256, 0, st, one, many, f[BK_ZERO], ntasks);
+    launch_k(count_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
+    launch_k(scan_reduce_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
+    launch_k(scan_tiles_kernel<MULTI>, g.total[BK_ONE], 1024, 0, st, one, many, f[BK_ONE], ntasks);
+    launch_k(scan_down_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
+    launch_k(scatter_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
+    launch_k(sort_small_kernel<MULTI>, g.total[BK_SSMALL], 256, 0, st, one, many, f[BK_SSMALL], ntasks);
+    launch_k(sort_medium_kernel<MULTI>, g.total[BK_SMED], 512, 0, st, one, many, f[BK_SMED], ntasks);
+    launch_k(sort_large_kernel<MULTI>, g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, st, one, many,
+             f[BK_SLARGE], ntasks);
     if (g.total[BK_REFS] > 0) {
         count_launches(1);
-        cell_records_kernel<MULTI><<<g.total[BK_REFS], 256, 0, st>>>(one, many, f[BK_REFS], ntasks);
+        launch_k(cell_records_kernel<MULTI>, g.total[BK_REFS], 256, 0, st, one, many, f[BK_REFS], ntasks);
     }
 }
 

@@ -40,6 +40,22 @@ enum : uint32_t {
     ST_SORT_CAP = 32u,    // segmented-sort work lists overflowed
 };
 
+// Programmatic dependent launch (GRIDRT_PDL = 1): build and trace kernels are
+// launched with programmatic stream serialisation, so a kernel's blocks may
+// be scheduled while its predecessor drains; every such kernel first waits
+// (griddepcontrol.wait) until the predecessor has completed and its memory
+// is visible, then allows its own successor to start launching.  Without the
+// launch attribute both instructions return at once.
+#ifndef GRIDRT_PDL
+#define GRIDRT_PDL 0
+#endif
+__device__ __forceinline__ void pdl_begin() {
+#if GRIDRT_PDL
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+
 // Per-cell sort size classes: warp registers up to 32 entries, one warp's
 // shared-memory slice up to 256, a block above (bitonic up to 4096, bitmap
 // beyond).

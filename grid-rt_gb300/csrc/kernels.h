@@ -89,6 +89,26 @@ struct TraceTuning {
     int heavy_lanes = 32;  // lanes per deferred ray in that pass: 4, 8, 16 or 32
 };
 
+// Kernel launch with programmatic stream serialisation when GRIDRT_PDL is on
+// (the kernels call pdl_begin() first), a plain launch otherwise.
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+#if GRIDRT_PDL
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+#endif
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Per-launch device state of a single-scene trace: three counters the launch
 // zeroes (ray claims, deferred rays, deferred claims) and the deferred-ray
 // queue; launches that may overlap need distinct slots.

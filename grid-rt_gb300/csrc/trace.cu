@@ -555,6 +555,7 @@ __device__ __forceinline__ void flush_counters(TraceCounters* ctr, uint32_t star
 
 template <int MODE, bool COUNT, int ER>
 __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(SceneView s, TraceIO io) {
+    pdl_begin();
     __shared__ SParams P;
     load_sparams(s.params, P);
     const int lane = threadIdx.x & 31;
@@ -743,6 +744,7 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
 
 template <int MODE, bool COUNT, int G>
 __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io) {
+    pdl_begin();
     __shared__ SParams P;
     load_sparams(s.params, P);
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), grp = lane / G;
@@ -798,6 +800,7 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
     trace_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes, const BatchTask* __restrict__ tasks,
                        int ntasks, long long total, unsigned long long* counter, int2* defer, int32_t defer_cap,
                        int32_t heavy) {
+    pdl_begin();
     __shared__ SParams P[kMaxBatchScenes];
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
     __syncthreads();
@@ -837,6 +840,7 @@ __global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene*
                                                                const BatchTask* __restrict__ tasks, int ntasks,
                                                                unsigned long long* counter,
                                                                const int2* __restrict__ defer, int32_t defer_cap) {
+    pdl_begin();
     __shared__ SParams P[kMaxBatchScenes];
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
     __syncthreads();
@@ -910,6 +914,7 @@ __device__ __forceinline__ void xf_dir(const float* m, float x, float y, float z
 }
 
 __global__ void instances_prep_kernel(const InstanceRec* __restrict__ recs, int ninst, SParams* __restrict__ sp) {
+    pdl_begin();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ninst; i += gridDim.x * blockDim.x)
         fill_sparams(recs[i].view.params, sp[i]);
 }
@@ -918,6 +923,7 @@ template <int MODE, int ER>
 __global__ void __launch_bounds__(128) trace_instances_kernel(const InstanceRec* __restrict__ recs,
                                                               const SParams* __restrict__ sp, int ninst,
                                                               InstanceBox box, TraceIO io, int32_t* inst_out) {
+    pdl_begin();
     __shared__ SParams Pw[4];
     const int lane = threadIdx.x & 31;
     SParams& P = Pw[threadIdx.x >> 5];
@@ -1073,6 +1079,7 @@ void launch_trace_instances(const InstanceRec* recs, void* d_params, int ninst, 
 
 __global__ void deform_kernel(const float* __restrict__ base, const float* __restrict__ nrm, float* __restrict__ out,
                               int64_t nverts, float amp, float freq, float phase) {
+    pdl_begin();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nverts; i += stride) {
         const float px = base[3 * i], py = base[3 * i + 1], pz = base[3 * i + 2];
@@ -1098,7 +1105,7 @@ static void launch_er(const SceneView& s, const TraceIO& io, const TraceTuning& 
     if (tune.persistent) blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
     if (blocks < 1) blocks = 1;
     if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
-    trace_kernel<MODE, COUNT, ER><<<(int)blocks, 128, 0, st>>>(s, io);
+    launch_k(trace_kernel<MODE, COUNT, ER>, (unsigned)blocks, 128, 0, st, s, io);
 }
 
 template <int MODE, bool COUNT>
@@ -1118,7 +1125,7 @@ static void launch_wide_g(const SceneView& s, const TraceIO& io, int num_sms, cu
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_kernel<MODE, COUNT, G>, 128, 0);
         per_sm = b > 0 ? b : 1;
     }
-    trace_wide_kernel<MODE, COUNT, G><<<per_sm * num_sms, 128, 0, st>>>(s, io);
+    launch_k(trace_wide_kernel<MODE, COUNT, G>, (unsigned)(per_sm * num_sms), 128, 0, st, s, io);
 }
 
 template <int MODE, bool COUNT>
@@ -1201,8 +1208,8 @@ static void launch_batch_er(const BatchScene* scenes, int nscenes, const BatchTa
     long long blocks = (total + 127) / 128;
     blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
     if (blocks < 1) blocks = 1;
-    trace_batch_kernel<ER><<<(int)blocks, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, total, slot.ctr,
-                                                         heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy);
+    launch_k(trace_batch_kernel<ER>, (unsigned)blocks, 128, 0, st, scenes, nscenes, tasks, ntasks, total, slot.ctr,
+             heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy);
 }
 
 template <int G>
@@ -1214,8 +1221,8 @@ static void launch_wide_batch(const BatchScene* scenes, int nscenes, const Batch
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_wide_batch_kernel<G>, 128, 0);
         per_sm = b > 0 ? b : 1;
     }
-    trace_wide_batch_kernel<G><<<per_sm * num_sms, 128, 0, st>>>(scenes, nscenes, tasks, ntasks, slot.ctr,
-                                                                  slot.defer, slot.defer_cap);
+    launch_k(trace_wide_batch_kernel<G>, (unsigned)(per_sm * num_sms), 128, 0, st, scenes, nscenes, tasks, ntasks,
+             slot.ctr, slot.defer, slot.defer_cap);
 }
 
 void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
@@ -1244,7 +1251,7 @@ void launch_deform(const float* base, const float* normals, float* out, int64_t 
     count_launches(1);
     int64_t blocks = (nverts + 255) / 256;
     if (blocks > 4096) blocks = 4096;
-    deform_kernel<<<(int)blocks, 256, 0, st>>>(base, normals, out, nverts, amp, freq, phase);
+    launch_k(deform_kernel, (unsigned)blocks, 256, 0, st, base, normals, out, nverts, amp, freq, phase);
 }
 
 }  // namespace gridrt
