@@ -45,9 +45,11 @@ enum : uint32_t {
 // be scheduled while its predecessor drains; every such kernel first waits
 // (griddepcontrol.wait) until the predecessor has completed and its memory
 // is visible, then allows its own successor to start launching.  Without the
-// launch attribute both instructions return at once.
+// launch attribute both instructions return at once.  On by default: frames
+// launched call by call run 5% faster (0.459 -> 0.437 ms, deforming sphere
+// k = 2); graph-replayed frames are unchanged.
 #ifndef GRIDRT_PDL
-#define GRIDRT_PDL 0
+#define GRIDRT_PDL 1
 #endif
 __device__ __forceinline__ void pdl_begin() {
 #if GRIDRT_PDL
