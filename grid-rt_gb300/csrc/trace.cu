@@ -28,12 +28,6 @@ namespace gridrt {
 static constexpr unsigned FULL = 0xffffffffu;
 static constexpr int32_t kDeferred = -3;    // Lane::id of a ray handed to the warp-per-ray pass
 static constexpr int32_t kNoHeavy = 0x7fffffff;
-static constexpr int32_t kHandback = -4;    // Lane::id of a ray the group pass leaves to the one-lane pass
-// GRIDRT_HANDBACK = 1: the group pass tests only the long lists of a deferred
-// ray and hands the rest of its walk back to a one-lane pass.
-#ifndef GRIDRT_HANDBACK
-#define GRIDRT_HANDBACK 1
-#endif
 // A ray is also deferred once its tests would pass kHeavyWorkMult x the
 // heavy-cell threshold in total (0: only long lists defer).
 #ifndef GRIDRT_HEAVY_WORK_MULT
@@ -672,15 +666,11 @@ __device__ __forceinline__ void resume_at(const SParams& P, Lane& L, int32_t cel
 // Walks the group's ray (state in L, identical on its G lanes) to its end.
 // Every lane of the warp calls it; groups that are done idle through the
 // warp-wide list loop and reductions.
-// handback: after the first cell, the group stops at a non-empty cell whose
-// list is not longer than this (kNoHeavy: never) and leaves the ray there for
-// the one-lane pass (L.id = kHandback, the cell not counted).
 template <int G>
 __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
-                                          int32_t handback, uint32_t& cells, uint32_t& tests) {
+                                          uint32_t& cells, uint32_t& tests) {
     const int gl = threadIdx.x & (G - 1);
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
-    bool first = true;
     while (__any_sync(FULL, !done)) {
         int32_t b = 0, e = 0;
         float hi = 0.0f;
@@ -691,16 +681,8 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
                 const int32_t c = L.x + L.y * nx + L.z * nxy;
                 b = __ldg(s.offsets + c);
                 e = __ldg(s.offsets + c + 1);
-                if (!first && e - b <= handback) {
-                    if (gl == 0) --cells;
-                    L.id = kHandback;
-                    done = true;
-                    b = e = 0;
-                } else {
-                    hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-                    if (gl == 0) tests += (uint32_t)(e - b);
-                }
-                first = false;
+                hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+                if (gl == 0) tests += (uint32_t)(e - b);
             }
         }
         const unsigned trips = __reduce_max_sync(FULL, (unsigned)((e - b + G - 1) / G));
@@ -760,46 +742,6 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
     }
 }
 
-// The one-lane pass over rays the group pass handed back: each lane resumes
-// its ray at the recorded cell and walks it to the end without deferral.
-template <int MODE, bool COUNT, int ER>
-__global__ void __launch_bounds__(128) trace_resume_kernel(SceneView s, TraceIO io) {
-    pdl_begin();
-    __shared__ SParams P;
-    load_sparams(s.params, P);
-    const int lane = threadIdx.x & 31;
-    unsigned long long nd = io.counter[1];
-    if (nd > (unsigned long long)io.defer_cap) nd = (unsigned long long)io.defer_cap;
-    uint32_t cells = 0, tests = 0;
-    for (;;) {
-        unsigned long long j0 = 0;
-        if (lane == 0) j0 = atomicAdd(io.counter + 3, 32ull);
-        j0 = __shfl_sync(FULL, j0, 0);
-        if (j0 >= nd) break;
-        const unsigned long long j = j0 + lane;
-        Lane L;
-        bool active = false;
-        if (j < nd) {
-            const int2 d = io.defer[j];
-            if (d.x >= 0) {
-                L.ray = d.x;
-                if (start_ray<MODE>(P, io, L, L.ray)) {
-                    resume_at(P, L, d.y);
-                    active = true;
-                }
-            }
-        }
-        while (__any_sync(FULL, active)) {
-            if (active && advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, s.crec, kNoHeavy, kNoHeavy, cells,
-                                            tests)) {
-                finish_ray<MODE>(io, P, s.tris, L);
-                active = false;
-            }
-        }
-    }
-    if (COUNT) flush_counters(io.ctr, 0, cells, tests);
-}
-
 template <int MODE, bool COUNT, int G>
 __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io) {
     pdl_begin();
@@ -830,16 +772,8 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
                 resume_at(P, L, d.y);
             }
         }
-        wide_walk<G>(P, s, L, done, MODE == MODE_ANY, GRIDRT_HANDBACK ? io.heavy : kNoHeavy, cells, tests);
-        if (valid && gl == 0) {
-            if (L.id == kHandback) {
-                // the one-lane pass resumes the ray at this cell
-                io.defer[j] = make_int2(L.ray, L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
-            } else {
-                io.defer[j].x = -1;
-                finish_ray<MODE>(io, P, s.tris, L);
-            }
-        }
+        wide_walk<G>(P, s, L, done, MODE == MODE_ANY, cells, tests);
+        if (valid && gl == 0) finish_ray<MODE>(io, P, s.tris, L);
     }
     if (COUNT) {
         if (gl != 0) cells = tests = 0;
@@ -949,7 +883,7 @@ __global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene*
             }
         }
         const SceneView V = scenes[scene].view;
-        wide_walk<G>(P[scene], V, L, done, any, kNoHeavy, cells, tests);
+        wide_walk<G>(P[scene], V, L, done, any, cells, tests);
         if (valid && gl == 0) {
             if (any) finish_ray<MODE_ANY>(io, P[scene], V.tris, L);
             else finish_ray<MODE_NEAREST>(io, P[scene], V.tris, L);
@@ -1203,26 +1137,6 @@ static void launch_wide(const SceneView& s, const TraceIO& io, const TraceTuning
     else launch_wide_g<MODE, COUNT, 32>(s, io, num_sms, st);
 }
 
-template <int MODE, bool COUNT, int ER>
-static void launch_resume_er(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
-    static int per_sm = 0;
-    if (per_sm == 0) {
-        int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_resume_kernel<MODE, COUNT, ER>, 128, 0);
-        per_sm = b > 0 ? b : 1;
-    }
-    launch_k(trace_resume_kernel<MODE, COUNT, ER>, (unsigned)(per_sm * num_sms), 128, 0, st, s, io);
-}
-
-template <int MODE, bool COUNT>
-static void launch_resume(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms,
-                          cudaStream_t st) {
-    if (tune.empty_run <= 2) launch_resume_er<MODE, COUNT, 2>(s, io, num_sms, st);
-    else if (tune.empty_run <= 4) launch_resume_er<MODE, COUNT, 4>(s, io, num_sms, st);
-    else if (tune.empty_run <= 8) launch_resume_er<MODE, COUNT, 8>(s, io, num_sms, st);
-    else launch_resume_er<MODE, COUNT, 16>(s, io, num_sms, st);
-}
-
 template <int MODE>
 static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, const TraceTuning& tune, int num_sms,
                         cudaStream_t st) {
@@ -1231,17 +1145,13 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.defer = defer ? slot.defer : nullptr;
     io.defer_cap = defer ? slot.defer_cap : 0;
     io.heavy = defer ? tune.heavy_cell : kNoHeavy;
-    count_launches(defer ? (GRIDRT_HANDBACK ? 3 : 2) : 1);
-    cudaMemsetAsync(slot.ctr, 0, 4 * sizeof(unsigned long long), st);
+    count_launches(defer ? 2 : 1);
+    cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {
         if (io.ctr) launch_wide<MODE, true>(s, io, tune, num_sms, st);
         else launch_wide<MODE, false>(s, io, tune, num_sms, st);
-        if (GRIDRT_HANDBACK) {
-            if (io.ctr) launch_resume<MODE, true>(s, io, tune, num_sms, st);
-            else launch_resume<MODE, false>(s, io, tune, num_sms, st);
-        }
     }
 }
 
