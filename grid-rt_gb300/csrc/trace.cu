@@ -128,6 +128,10 @@ __device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear
     return true;
 }
 
+#ifndef GRIDRT_EXIT_ALL
+#define GRIDRT_EXIT_ALL 0
+#endif
+
 // One DDA step (src/rtplugins/UniformGridAccStruct.cpp:179-195): the strict-<
 // axis choice and a step of vr::sign(direction).  The reference then exits
 // when x == outX (or y, z), with out = -1 for a negative direction sign bit and
@@ -136,18 +140,27 @@ __device__ __forceinline__ bool setup_ray(const SParams& P, Lane& L, float tnear
 // coordinate leaves [0, n): the test below is the same predicate.  True when
 // the walk has left the grid.
 __device__ __forceinline__ bool dda_step(const SParams& P, Lane& L) {
+    // the other two coordinates did not move and were inside: only the moved
+    // one can have left the grid
+    bool out;
     if (L.tMx < L.tMy && L.tMx < L.tMz) {
         L.x += L.dx < 0.0f ? -1 : (L.dx > 0.0f ? 1 : 0);
         L.tMx = fadd(L.tMx, L.tDx);
+        out = (unsigned)L.x >= (unsigned)P.res[0];
     } else if (L.tMy < L.tMz) {
         L.y += L.dy < 0.0f ? -1 : (L.dy > 0.0f ? 1 : 0);
         L.tMy = fadd(L.tMy, L.tDy);
+        out = (unsigned)L.y >= (unsigned)P.res[1];
     } else {
         L.z += L.dz < 0.0f ? -1 : (L.dz > 0.0f ? 1 : 0);
         L.tMz = fadd(L.tMz, L.tDz);
+        out = (unsigned)L.z >= (unsigned)P.res[2];
     }
-    return (unsigned)L.x >= (unsigned)P.res[0] || (unsigned)L.y >= (unsigned)P.res[1] ||
-           (unsigned)L.z >= (unsigned)P.res[2] || --L.budget <= 0;
+#if GRIDRT_EXIT_ALL
+    out = (unsigned)L.x >= (unsigned)P.res[0] || (unsigned)L.y >= (unsigned)P.res[1] ||
+          (unsigned)L.z >= (unsigned)P.res[2];
+#endif
+    return out || --L.budget <= 0;
 }
 
 // Moller-Trumbore test of one triangle record against the lane's ray with the
