@@ -343,6 +343,13 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
     cudaFree(s->d_io);
     cudaFree(s->d_ctr);
     cudaFree(s->d_verts_back);
+    if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
+    cudaFree(s->d_fring);
+    for (int i = 0; i < 2; ++i) {
+        if (s->frame_traced[i]) cudaEventDestroy(s->frame_traced[i]);
+        if (s->frame_copied[i]) cudaEventDestroy(s->frame_copied[i]);
+    }
+    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->staged_ev) cudaEventDestroy(s->staged_ev);
     if (s->build_ev) cudaEventDestroy(s->build_ev);
     if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -806,6 +813,58 @@ rtg_status rtg_trace_frame(rtg_scene s, const rtg_camera* cam, const float* ligh
     CUDA_TRY(cudaMemcpyAsync(hits, d_hits, n * 16, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(occluded, d_occ, n, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_frame_async(rtg_scene s, const rtg_camera* cam, const float* light_pos, rtg_hit* hits,
+                                 uint8_t* occluded, void* stream, uint64_t* ticket) {
+    rtg_status rc = check_traceable(s, 0);
+    if (rc) return rc;
+    if (!camera_ok(cam)) return fail(RTG_INVALID_PARAM, "bad camera");
+    if (!light_pos || !hits || !occluded || !ticket) return fail(RTG_INVALID_PARAM, "NULL arguments");
+    if (!s->copy_stream) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            CUDA_TRY(cudaEventCreateWithFlags(&s->frame_traced[i], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&s->frame_copied[i], cudaEventDisableTiming));
+        }
+    }
+    const int64_t n = (int64_t)cam->width * cam->height;
+    const int64_t sr_bytes = (32 * n + 255) & ~(int64_t)255;
+    const int64_t hit_bytes = (16 * n + 255) & ~(int64_t)255;
+    const int64_t slot_bytes = hit_bytes + ((n + 255) & ~(int64_t)255);
+    cudaStream_t st = pick(s, stream);
+    if (sr_bytes + 2 * slot_bytes > s->fring_cap) {
+        // a larger frame: no earlier frame of this scene may still use the ring
+        CUDA_TRY(cudaStreamSynchronize(st));
+        CUDA_TRY(cudaStreamSynchronize(s->copy_stream));
+        CUDA_TRY(grow(s->d_fring, s->fring_cap, sr_bytes + 2 * slot_bytes));
+    }
+    const int slot = (int)(s->frame_seq & 1);
+    float* d_sr = reinterpret_cast<float*>(s->d_fring);
+    rtg_hit* d_hits = reinterpret_cast<rtg_hit*>(s->d_fring + sr_bytes + slot * slot_bytes);
+    uint8_t* d_occ = s->d_fring + sr_bytes + slot * slot_bytes + hit_bytes;
+    // the slot's previous frame must be copied out before this one overwrites it
+    if (s->frame_seq >= 2) CUDA_TRY(cudaStreamWaitEvent(st, s->frame_copied[slot], 0));
+    rc = rtg_trace_frame_device(s, cam, light_pos, d_hits, d_occ, d_sr, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(s->frame_traced[slot], st));
+    CUDA_TRY(cudaStreamWaitEvent(s->copy_stream, s->frame_traced[slot], 0));
+    CUDA_TRY(cudaMemcpyAsync(hits, d_hits, n * 16, cudaMemcpyDeviceToHost, s->copy_stream));
+    CUDA_TRY(cudaMemcpyAsync(occluded, d_occ, n, cudaMemcpyDeviceToHost, s->copy_stream));
+    CUDA_TRY(cudaEventRecord(s->frame_copied[slot], s->copy_stream));
+    *ticket = s->frame_seq++;
+    return RTG_OK;
+}
+
+rtg_status rtg_trace_frame_wait(rtg_scene s, uint64_t ticket) {
+    if (!s) return fail(RTG_INVALID_PARAM, "scene is NULL");
+    if (ticket >= s->frame_seq) return fail(RTG_INVALID_PARAM, "no frame with this ticket was enqueued");
+    rtg_status rc = set_device(s);
+    if (rc) return rc;
+    // copies finish in order on the copy stream; the slot's event marks this
+    // frame's copy or a later one
+    CUDA_TRY(cudaEventSynchronize(s->frame_copied[ticket & 1]));
     return RTG_OK;
 }
 

@@ -60,6 +60,14 @@ struct rtg_scene_s {
 
     unsigned char* d_io = nullptr;
     int64_t io_cap = 0;
+    // rtg_trace_frame_async: shadow-ray area + two output slots, copied back
+    // on copy_stream; frame_copied[i] marks the end of slot i's last copy
+    unsigned char* d_fring = nullptr;
+    int64_t fring_cap = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t frame_traced[2] = {nullptr, nullptr};
+    cudaEvent_t frame_copied[2] = {nullptr, nullptr};
+    uint64_t frame_seq = 0;              // frames enqueued so far
     gridrt::TraceCounters* d_ctr = nullptr;
 };
 

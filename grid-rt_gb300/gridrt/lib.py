@@ -141,7 +141,8 @@ EXPORTS = [
     "rtg_scene_deform_vertices", "rtg_scene_build", "rtg_scene_build_async", "rtg_scene_build_check",
     "rtg_scene_reserve", "rtg_scene_grid_info", "rtg_scene_grid_download", "rtg_scene_download_vertices", "rtg_scene_grid_device",
     "rtg_trace_nearest", "rtg_trace_nearest_device", "rtg_trace_any", "rtg_trace_any_device",
-    "rtg_trace_camera_device", "rtg_trace_camera_diffuse_device", "rtg_trace_frame_device", "rtg_trace_frame", "rtg_grid_build_noalloc",
+    "rtg_trace_camera_device", "rtg_trace_camera_diffuse_device", "rtg_trace_frame_device", "rtg_trace_frame",
+    "rtg_trace_frame_async", "rtg_trace_frame_wait", "rtg_grid_build_noalloc",
     "rtg_kernel_launch_count",
     "rtg_scene_set_tuning", "rtg_scene_counters", "rtg_batch_create", "rtg_batch_build_async",
     "rtg_batch_trace_async", "rtg_batch_check", "rtg_batch_rays", "rtg_batch_set_tuning", "rtg_batch_destroy",
@@ -197,6 +198,8 @@ def load(build_if_missing: bool = True):
         "rtg_trace_camera_diffuse_device": ([vp, C.POINTER(CameraC), C.c_uint64, vp, vp, i32, vp], C.c_int),
         "rtg_trace_frame_device": ([vp, C.POINTER(CameraC), vp, vp, vp, vp, vp], C.c_int),
         "rtg_trace_frame": ([vp, C.POINTER(CameraC), vp, vp, vp, vp], C.c_int),
+        "rtg_trace_frame_async": ([vp, C.POINTER(CameraC), vp, vp, vp, vp, C.POINTER(C.c_uint64)], C.c_int),
+        "rtg_trace_frame_wait": ([vp, C.c_uint64], C.c_int),
         "rtg_grid_build_noalloc": ([vp, i64, vp, i64, i32, vp, i64, vp, i64, vp, C.POINTER(GridInfo), vp],
                                    C.c_int),
         "rtg_kernel_launch_count": ([], C.c_uint64),
@@ -417,6 +420,20 @@ class Scene:
         self._light = np.ascontiguousarray(light, np.float32)
         check(load().rtg_trace_frame(self.h, C.byref(cs), _ptr(self._light), _ptr(hits_host), _ptr(occ_host),
                                      stream))
+
+    def trace_frame_async(self, cam, light, hits_host, occ_host, order: str = "scanline", stream=None) -> int:
+        """trace_frame without waiting: returns the frame's ticket; the host
+        buffers (pinned, kept alive by the caller) are complete after
+        trace_frame_wait(ticket)."""
+        cs = camera_struct(cam, order)
+        self._light = np.ascontiguousarray(light, np.float32)
+        t = C.c_uint64(0)
+        check(load().rtg_trace_frame_async(self.h, C.byref(cs), _ptr(self._light), _ptr(hits_host), _ptr(occ_host),
+                                           stream, C.byref(t)))
+        return int(t.value)
+
+    def trace_frame_wait(self, ticket: int):
+        check(load().rtg_trace_frame_wait(self.h, int(ticket)))
 
     def set_tuning(self, empty_run: int = None, persistent: bool = None, cell_records: bool = None,
                    heavy_cell: int = None, heavy_lanes: int = None):

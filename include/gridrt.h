@@ -202,6 +202,23 @@ rtg_status rtg_trace_frame_device(rtg_scene scene, const rtg_camera* cam, const 
 rtg_status rtg_trace_frame(rtg_scene scene, const rtg_camera* cam, const float* light_pos, rtg_hit* hits,
                            uint8_t* occluded, void* stream);
 
+/* rtg_trace_frame for a frame loop, the frame-level render of
+ * src/rtcuda/CudaRenderer.cpp:33-63 with its read-back overlapped: enqueues
+ * the frame's two trace passes on `stream` and the copy of hits and
+ * occlusion into the host buffers on a copy stream of the scene, and
+ * returns without waiting; *ticket receives the frame's number (0, 1, ...).
+ * The copy overlaps the next frames' builds and traces when the host
+ * buffers are pinned (cudaMallocHost); with pageable buffers it is correct
+ * but not overlapped.  Two frames' device outputs alternate: a frame's trace
+ * waits, on the GPU, for the copy of the frame two before it.  The host
+ * buffers are complete once rtg_trace_frame_wait(scene, ticket) returns and
+ * must stay valid until then.  Enqueue a scene's frames on one stream. */
+rtg_status rtg_trace_frame_async(rtg_scene scene, const rtg_camera* cam, const float* light_pos, rtg_hit* hits,
+                                 uint8_t* occluded, void* stream, uint64_t* ticket);
+/* Blocks until the frame with this ticket, and every frame before it, is in
+ * its host buffers.  RTG_INVALID_PARAM for a ticket not yet issued. */
+rtg_status rtg_trace_frame_wait(rtg_scene scene, uint64_t ticket);
+
 /* Grid build that allocates no device memory.  It has no counterpart in the
  * reference; it exists for callers that must not let a library allocate GPU
  * memory: real-time frame loops, where an allocation and the synchronisation

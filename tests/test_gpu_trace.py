@@ -252,3 +252,43 @@ def test_diffuse_secondary_rays(gridlib, oracle):
     s.trace_camera_diffuse_device(cam, 1234, d_hits, d_sec2, order="morton8")
     torch.cuda.synchronize()
     assert torch.equal(d_sec, d_sec2)
+
+
+def test_frame_async_matches_frame(gridlib):
+    """rtg_trace_frame_async: frames of changing keyframes enqueued two
+    ahead of the host's wait, into alternating pinned buffers, give exactly
+    the synchronous rtg_trace_frame results of their keyframes."""
+    import torch
+    v, idx, nrm = scenes.sphere_mesh(40, 80)
+    s = gridlib.Scene(0)
+    s.set_geometry(v, idx)
+    cam = scenes.deforming_sphere_camera(256, 256)
+    n = cam.width * cam.height
+    light = scenes.SPHERE_LIGHT
+    keys = [np.ascontiguousarray(scenes.deform(v, nrm, f), np.float32) for f in range(3)]
+    ref = []
+    for kv in keys:
+        s.update_vertices(kv, kv.shape[0], False)
+        s.build(4)
+        h, o = np.empty((n, 4), np.int32), np.empty(n, np.uint8)
+        s.trace_frame(cam, light, h, o, order="morton8")
+        ref.append((h, o))
+    hits = [torch.empty((n, 4), dtype=torch.int32).pin_memory() for _ in range(2)]
+    occ = [torch.empty(n, dtype=torch.uint8).pin_memory() for _ in range(2)]
+    tickets = []
+    for i in range(7):
+        s.update_vertices(keys[i % 3], keys[i % 3].shape[0], False)
+        s.build_async(4)
+        tickets.append(s.trace_frame_async(cam, light, hits[i % 2], occ[i % 2], order="morton8"))
+        if i:
+            s.trace_frame_wait(tickets[i - 1])
+            h, o = ref[(i - 1) % 3]
+            assert np.array_equal(hits[(i - 1) % 2].numpy(), h), i - 1
+            assert np.array_equal(occ[(i - 1) % 2].numpy(), o), i - 1
+    s.trace_frame_wait(tickets[-1])
+    h, o = ref[6 % 3]
+    assert np.array_equal(hits[0].numpy(), h) and np.array_equal(occ[0].numpy(), o)
+    assert tickets == list(range(7))
+    assert (ref[0][1] != 2).sum() > 0          # the frames have shadow rays
+    with pytest.raises(gridlib.GridRTError):
+        s.trace_frame_wait(7)
