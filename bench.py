@@ -1124,6 +1124,33 @@ def run_serving(args, rank, ws, local, dist):
     sat = make_requests(None, args.serve_saturation, 7)
     saturation = {"served": run(sat, False), "plain": run(sat, True),
                   "plain_pipelined": run(sat, True, in_flight=3)}
+
+    # device-only ceiling: the saturation requests' rays already in HBM,
+    # traced as one batch launch (no transfers, no request loop, no waits)
+    dev = torch.device("cuda", local)
+    d_src = {h_near.data_ptr(): h_near.to(dev), h_any.data_ptr(): h_any.to(dev)}
+    tasks = []
+    for (_, si, mode, ptr, n, _) in sat:
+        hsrc = h_any if mode == lib.RTG_MODE_ANY else h_near
+        d_rays = d_src[hsrc.data_ptr()].data_ptr() + (ptr - hsrc.data_ptr())
+        d_out = torch.empty(n * (1 if mode == lib.RTG_MODE_ANY else 16), dtype=torch.uint8, device=dev)
+        tasks.append((si, mode, d_rays, n, d_out))
+    ceil_batch = lib.Batch(scs, [4] * nscenes, tasks)
+    st = torch.cuda.Stream(device=dev)
+    ceil_batch.trace_async(st.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(st):
+        e0.record(st)
+        ceil_batch.trace_async(st.cuda_stream)
+        e1.record(st)
+    torch.cuda.synchronize()
+    ceil_ms = e0.elapsed_time(e1)
+    saturation["device_ceiling"] = {"mrays_s": round(saturation["served"]["rays"] / ceil_ms / 1e3, 2),
+                                    "ms": round(ceil_ms, 3),
+                                    "how": "the same requests' rays resident in HBM, one rtg_batch trace launch "
+                                           "over all of them (no copies, no request loop)"}
+    del ceil_batch, tasks, d_src
     if rank != 0:
         return
     print(json.dumps({
