@@ -797,7 +797,8 @@ def run_skewed(args, rank, ws, local, dist):
         best, allres = dict(fixed), []
     else:
         space = {"k": LAMBDAS, "order": ("scanline", "morton8"), "empty_run": (2, 4, 8), "persistent": (True,),
-                 "heavy_cell": (0, 24, 48), "heavy_lanes": (16, 32), "cell_records": (False, True)}
+                 "heavy_cell": (0, 24, 48), "heavy_lanes": (16, 32), "cell_records": (False, True),
+                 "refill": (0, 16)}
         best, allres = autotune.search(measure, space=space, reps=2)
     _apply_tuning(s, best)
     k, order = best["k"], best["order"]
@@ -1170,21 +1171,22 @@ def run_serving(args, rank, ws, local, dist):
 
 
 def _parse_tuning(text):
-    """'k=8,order=morton8,empty_run=4,persistent=0,heavy_cell=32,cell_records=1' -> dict, or None."""
+    """'k=8,order=morton8,empty_run=4,persistent=0,heavy_cell=32,cell_records=1,refill=16' -> dict, or None."""
     if not text:
         return None
     d = dict(kv.split("=", 1) for kv in text.split(","))
     yes = lambda v: v not in ("0", "false", "False")
     return {"k": int(d.get("k", 8)), "order": d.get("order", "morton8"), "empty_run": int(d.get("empty_run", 4)),
             "persistent": yes(d.get("persistent", "0")), "heavy_cell": int(d.get("heavy_cell", 0)),
-            "heavy_lanes": int(d.get("heavy_lanes", 32)), "cell_records": yes(d.get("cell_records", "0"))}
+            "heavy_lanes": int(d.get("heavy_lanes", 32)), "cell_records": yes(d.get("cell_records", "0")),
+            "refill": int(d.get("refill", 0))}
 
 
 def _apply_tuning(scene, cfg):
     """Launch-shape settings of one candidate; cell records take effect at the next build."""
     scene.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"],
                      heavy_cell=cfg.get("heavy_cell", 0), heavy_lanes=cfg.get("heavy_lanes", 32),
-                     cell_records=cfg.get("cell_records", False))
+                     cell_records=cfg.get("cell_records", False), refill=cfg.get("refill", 0))
 
 
 def main():

@@ -1137,6 +1137,10 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
             s->tune.cell_records = value ? 1 : 0;
             if (!value) s->crec_built = false;
             return RTG_OK;
+        case RTG_TUNE_REFILL:
+            if (value < 0 || value > 32) return fail(RTG_INVALID_PARAM, "refill threshold must be 0..32");
+            s->tune.refill = value;
+            return RTG_OK;
         default:
             return fail(RTG_INVALID_PARAM, "unknown tuning key");
     }

@@ -369,6 +369,7 @@ struct TraceIO {
     int32_t defer_cap;
     int32_t heavy;                 // lists longer than this are deferred (kNoHeavy: never)
     int32_t defer_base;            // added to a deferred ray's index (a batch task's first)
+    int32_t refill;                // > 0: lane refill at this many idle lanes (trace_refill)
 };
 
 // Loads ray `r` into the lane; false when the ray ends at once (misses the
@@ -555,31 +556,21 @@ __device__ __forceinline__ void flush_counters(TraceCounters* ctr, uint32_t star
 #define GRIDRT_TRACE_MIN_BLOCKS 8
 #endif
 
-// GRIDRT_REFILL = 1: instead of tracing a claimed batch of 32 rays to its
-// end, the warp hands new rays to its idle lanes whenever at least
-// GRIDRT_REFILL_MIN of them are idle (one claim for all of them), keeping the
-// lanes busy while a batch's long rays finish.
-#ifndef GRIDRT_REFILL
-#define GRIDRT_REFILL 0
-#endif
-#ifndef GRIDRT_REFILL_MIN
-#define GRIDRT_REFILL_MIN 16
-#endif
-
-template <int MODE, bool COUNT, int ER>
-__global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(SceneView s, TraceIO io) {
-    pdl_begin();
-    __shared__ SParams P;
-    load_sparams(s.params, P);
+// Lane refill (TraceIO::refill > 0): instead of tracing a claimed batch of
+// 32 rays to its end, the warp hands new rays to its idle lanes whenever at
+// least `refill` of them are idle (one claim for all of them), keeping the
+// lanes busy while long rays finish.  Pays on incoherent rays, whose walks
+// differ most in length (diffuse secondaries: -11% trace time); costs ~2% on
+// coherent camera rays, so it is a tuning choice.
+template <int MODE, int ER>
+__device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& s, const TraceIO& io, Lane& L,
+                                             uint32_t& cells, uint32_t& tests, uint32_t& started) {
     const int lane = threadIdx.x & 31;
-    Lane L;
-    uint32_t cells = 0, tests = 0, started = 0;
-#if GRIDRT_REFILL
     bool active = false, exhausted = false;
     int32_t heavy = io.heavy, work_cap = kNoHeavy;
     for (;;) {
         const unsigned idle = __ballot_sync(FULL, !active);
-        if (!exhausted && (__popc(idle) >= GRIDRT_REFILL_MIN || idle == FULL)) {
+        if (!exhausted && ((int)__popc(idle) >= io.refill || idle == FULL)) {
             const unsigned need = (unsigned)__popc(idle);
             unsigned long long b = 0;
             if (lane == 0) b = atomicAdd(io.counter, (unsigned long long)need);
@@ -636,16 +627,28 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(Sce
             active = false;
         }
     }
-#else
-    for (;;) {
-        // the warp claims the next 32 consecutive rays and traces them to the end
-        unsigned long long b = 0;
-        if (lane == 0) b = atomicAdd(io.counter, 32ull);
-        b = __shfl_sync(FULL, b, 0);
-        if ((long long)b >= io.n) break;
-        trace_batch32<MODE, ER>(P, s, io, L, (long long)b, cells, tests, started);
+}
+
+template <int MODE, bool COUNT, int ER>
+__global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(SceneView s, TraceIO io) {
+    pdl_begin();
+    __shared__ SParams P;
+    load_sparams(s.params, P);
+    const int lane = threadIdx.x & 31;
+    Lane L;
+    uint32_t cells = 0, tests = 0, started = 0;
+    if (io.refill > 0) {
+        trace_refill<MODE, ER>(P, s, io, L, cells, tests, started);
+    } else {
+        for (;;) {
+            // the warp claims the next 32 consecutive rays and traces them to the end
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(io.counter, 32ull);
+            b = __shfl_sync(FULL, b, 0);
+            if ((long long)b >= io.n) break;
+            trace_batch32<MODE, ER>(P, s, io, L, (long long)b, cells, tests, started);
+        }
     }
-#endif
     if (COUNT) flush_counters(io.ctr, started, cells, tests);
 }
 
@@ -1158,6 +1161,7 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.defer = defer ? slot.defer : nullptr;
     io.defer_cap = defer ? slot.defer_cap : 0;
     io.heavy = defer ? tune.heavy_cell : kNoHeavy;
+    io.refill = tune.refill;
     count_launches(defer ? 2 : 1);
     cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);

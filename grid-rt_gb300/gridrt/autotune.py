@@ -3,7 +3,7 @@
 Searches the product of a small space exhaustively -- cells per triangle k,
 ray tile order (scanline / Morton 8x8), empty-cell run length, persistent vs
 one-shot trace grid, the list length above which a ray is finished by the
-warp-per-ray pass, cell-ordered triangle records -- timing each candidate with a caller-supplied
+warp-per-ray pass, cell-ordered triangle records, lane refill -- timing each candidate with a caller-supplied
 measurement (CUDA events on the scene's stream), and caches the winner in a
 JSON file keyed by a workload signature (triangles, rays, scene box extent),
 so a second run of the same workload skips the search.  None of these
@@ -28,6 +28,7 @@ SPACE = {
     "heavy_cell": (0, 32, 48),
     "heavy_lanes": (16, 32),
     "cell_records": (False, True),
+    "refill": (0, 16),
 }
 
 

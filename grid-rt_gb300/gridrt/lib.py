@@ -27,6 +27,7 @@ RTG_TUNE_PERSISTENT = 2
 RTG_TUNE_CELL_RECORDS = 3
 RTG_TUNE_HEAVY_CELL = 4
 RTG_TUNE_HEAVY_LANES = 5
+RTG_TUNE_REFILL = 6
 ORDER = {"scanline": 0, "morton8": 1}
 
 
@@ -436,7 +437,7 @@ class Scene:
         check(load().rtg_trace_frame_wait(self.h, int(ticket)))
 
     def set_tuning(self, empty_run: int = None, persistent: bool = None, cell_records: bool = None,
-                   heavy_cell: int = None, heavy_lanes: int = None):
+                   heavy_cell: int = None, heavy_lanes: int = None, refill: int = None):
         if empty_run is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:
@@ -447,6 +448,8 @@ class Scene:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_HEAVY_CELL, int(heavy_cell)))
         if heavy_lanes is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_HEAVY_LANES, int(heavy_lanes)))
+        if refill is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_REFILL, int(refill)))
 
     def counters(self, reset: bool = True):
         out = (C.c_int64 * 3)()

@@ -463,13 +463,17 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *                        second pass that traces it with a group of lanes (the list split
  *                        over them); default 32, 0 off.  Results are identical either way.
  *                        Costs 16 MB of device memory per scene (deferred-ray queues).
- *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8, 16, 32 (default) */
+ *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8, 16, 32 (default)
+ *   RTG_TUNE_REFILL      n in 1..32: a warp hands new rays to its idle lanes whenever at least
+ *                        n are idle, instead of finishing each batch of 32 rays first (pays on
+ *                        incoherent rays); default 0, off */
 enum {
     RTG_TUNE_EMPTY_RUN = 1,
     RTG_TUNE_PERSISTENT = 2,
     RTG_TUNE_CELL_RECORDS = 3,
     RTG_TUNE_HEAVY_CELL = 4,
-    RTG_TUNE_HEAVY_LANES = 5
+    RTG_TUNE_HEAVY_LANES = 5,
+    RTG_TUNE_REFILL = 6
 };
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 

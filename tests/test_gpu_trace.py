@@ -137,17 +137,18 @@ def test_counters_match_oracle(gridlib, oracle):
 
 
 def test_results_independent_of_launch_tuning(gridlib, oracle):
-    """Launch shape (empty-cell run, persistent vs one-shot grid) and ray order
-    never change a result bit."""
+    """Launch shape (empty-cell run, persistent vs one-shot grid, lane refill
+    threshold) never changes a result bit."""
     import torch
     sc = scenes.deforming_sphere(3)
     s = _scene(gridlib, sc, 4)
     cam = scenes.deforming_sphere_camera(256, 256)
     n = cam.width * cam.height
     ref = None
-    for er in (2, 4, 8, 16):
-        for persistent in (True, False):
-            s.set_tuning(empty_run=er, persistent=persistent)
+    for er, persistent, refill in [(e, p, 0) for e in (2, 4, 8, 16) for p in (True, False)] + \
+            [(e, p, r) for e in (2, 8) for p in (True, False) for r in (1, 16, 32)]:
+        if True:
+            s.set_tuning(empty_run=er, persistent=persistent, refill=refill)
             d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
             d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
             d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
@@ -158,7 +159,7 @@ def test_results_independent_of_launch_tuning(gridlib, oracle):
                 ref = out
             else:
                 for a, b in zip(ref, out):
-                    assert np.array_equal(a, b), (er, persistent)
+                    assert np.array_equal(a, b), (er, persistent, refill)
 
 
 def _frame(s, cam, order="morton8"):
@@ -183,12 +184,12 @@ def test_heavy_cell_deferral_is_exact(gridlib, oracle, heavy):
     cam = scenes.deforming_sphere_camera(1024, 1024) if heavy == 1 else scenes.deforming_sphere_camera(512, 512)
     s.set_tuning(heavy_cell=0, cell_records=False)
     ref = _frame(s, cam)
-    for crec, lanes in ((False, 8), (True, 4), (True, 16), (False, 32)):
-        s.set_tuning(heavy_cell=heavy, cell_records=crec, heavy_lanes=lanes)
+    for crec, lanes, refill in ((False, 8, 0), (True, 4, 16), (True, 16, 1), (False, 32, 8)):
+        s.set_tuning(heavy_cell=heavy, cell_records=crec, heavy_lanes=lanes, refill=refill)
         s.build(8)
         out = _frame(s, cam)
         for a, b in zip(ref, out):
-            assert np.array_equal(a, b), (heavy, crec, lanes)
+            assert np.array_equal(a, b), (heavy, crec, lanes, refill)
     # the nearest / any entry points on explicit rays agree as well
     rng = np.random.default_rng(11)
     rays = scenes.random_rays(rng, 50_000, (-1.2, -1.2, -1.2), (1.2, 1.2, 1.2))
@@ -198,8 +199,11 @@ def test_heavy_cell_deferral_is_exact(gridlib, oracle, heavy):
     rays_any = rays.copy()
     rays_any[:, 7] = 0.5
     o0 = s.trace_any(rays_any)
-    s.set_tuning(heavy_cell=heavy, cell_records=True)
+    s.set_tuning(heavy_cell=heavy, cell_records=True, refill=0)
     s.build(8)
+    assert np.array_equal(h0.view(np.int32), s.trace_nearest(rays).view(np.int32))
+    assert np.array_equal(o0, s.trace_any(rays_any))
+    s.set_tuning(refill=16)
     assert np.array_equal(h0.view(np.int32), s.trace_nearest(rays).view(np.int32))
     assert np.array_equal(o0, s.trace_any(rays_any))
 
