@@ -431,7 +431,8 @@ __global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const Build
 }
 
 // ---------------------------------------------------------------------------
-// scan of the per-cell counts (in place, inclusive), three phases
+// scan of the per-cell counts (in place, inclusive), two phases: tile sums,
+// then each tile scanned from the sum of the tiles before it
 // ---------------------------------------------------------------------------
 static constexpr int SCAN_THREADS = 256;
 static constexpr int SCAN_ITEMS = 16;
@@ -485,68 +486,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(BuildArgs one
     }
 }
 
-__device__ __forceinline__ void scan_tiles_body(GridParams* p, BuildWork* w, int64_t* __restrict__ tile_sums,
-                                                          int32_t* __restrict__ offsets, int64_t ref_cap, unsigned vbx, unsigned vgx) {
-    if (fatal(p->status)) return;
-    const int64_t C = p->ncells;
-    const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
-    __shared__ int64_t sh[33];
-    __shared__ int64_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int64_t b = 0; b < ntiles; b += blockDim.x) {
-        const int64_t i = b + threadIdx.x;
-        const int64_t v = i < ntiles ? tile_sums[i] : 0;
-        int64_t x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            int64_t y = __shfl_up_sync(FULL, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) sh[wid] = x;
-        __syncthreads();
-        if (wid == 0) {
-            int64_t w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int64_t y = __shfl_up_sync(FULL, w, o);
-                if (lane >= o) w += y;
-            }
-            sh[lane] = w;
-        }
-        __syncthreads();
-        const int64_t warp_excl = wid ? sh[wid - 1] : 0;
-        if (i < ntiles) tile_sums[i] = carry + warp_excl + x - v;   // exclusive tile prefix
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry += warp_excl + x;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const int64_t R = carry;
-        if (R != p->nrefs) raise_status(p, w, ST_BAD_RANGE);
-        if (R > ref_cap) raise_status(p, w, ST_REF_CAP);
-        if (R >= INT32_MAX) raise_status(p, w, ST_TOO_BIG);
-        offsets[C] = (int32_t)R;
-    }
-}
-
-template <bool MULTI>
-__global__ void __launch_bounds__(1024) scan_tiles_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
-                       int ntasks) {
-    pdl_begin();
-    if (MULTI) {
-        const int t = block_task(first, ntasks);
-        const BuildArgs& a = many[t];
-        scan_tiles_body(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
-    } else {
-        const BuildArgs& a = one;
-        scan_tiles_body(a.params, a.work, a.tile_sums, a.offsets, a.ref_cap, blockIdx.x, gridDim.x);
-    }
-}
-
-// In-place inclusive scan of each tile plus its prefix; queues cells that
-// hold two or more triangles for the segmented sort.
+// In-place inclusive scan of each tile plus the sum of the tiles before it
+// (each block adds those tile sums itself); queues cells that hold two or
+// more triangles for the segmented sort.  The block of the last tile writes
+// the reference total R = offsets[C] and checks it against the count pass
+// and the capacities.
 __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, GridParams* p,
-                                                                 const int64_t* __restrict__ tile_prefix,
+                                                                 const int64_t* __restrict__ tile_sums,
+                                                                 int64_t ref_cap,
                                                                  uint32_t* __restrict__ occ,
                                                                  BuildWork* w, int32_t* __restrict__ q_small,
                                                                  int32_t* __restrict__ q_med,
@@ -556,8 +503,12 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
     const int64_t C = p->ncells;
     const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ int64_t sh[9];
+    __shared__ int64_t shs[33];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int64_t tile = vbx; tile < ntiles; tile += vgx) {
+        int64_t before = 0;
+        for (int64_t j = threadIdx.x; j < tile; j += blockDim.x) before += tile_sums[j];
+        const int64_t prefix = block_sum_i64(before, shs);
         const int64_t b = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
         int32_t v[SCAN_ITEMS];
         int64_t s = 0;
@@ -582,7 +533,14 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             }
         }
         __syncthreads();
-        int64_t run = tile_prefix[tile] + sh[wid] + x - s;
+        int64_t run = prefix + sh[wid] + x - s;
+        if (tile == ntiles - 1 && threadIdx.x == SCAN_THREADS - 1) {
+            const int64_t R = run + s;   // the last thread's inclusive sum: the grand total
+            if (R != p->nrefs) raise_status(p, w, ST_BAD_RANGE);
+            if (R > ref_cap) raise_status(p, w, ST_REF_CAP);
+            if (R >= INT32_MAX) raise_status(p, w, ST_TOO_BIG);
+            counts[C] = (int32_t)R;
+        }
         __syncthreads();
         if (occ && s > 0 && b < C) {
             // occupancy bits of this thread's 16 consecutive cells (one row
@@ -668,10 +626,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_down_kernel(BuildArgs one, 
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
-        scan_down_body(a.offsets, a.params, a.tile_sums, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+        scan_down_body(a.offsets, a.params, a.tile_sums, a.ref_cap, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
     } else {
         const BuildArgs& a = one;
-        scan_down_body(a.offsets, a.params, a.tile_sums, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap, blockIdx.x, gridDim.x);
+        scan_down_body(a.offsets, a.params, a.tile_sums, a.ref_cap, a.occ, a.work, a.q_small, a.q_med, a.q_large, a.q_small_cap, a.q_med_cap, a.q_large_cap, blockIdx.x, gridDim.x);
     }
 }
 
@@ -961,7 +919,6 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     out[BK_ZERO] = clampi((a.cell_cap / 4 + 255) / 256, 8 * sms);
     out[BK_TRI] = clampi((a.ntris + 255) / 256, 16 * sms);            // one warp per 32 triangles
     out[BK_TILE] = clampi((a.cell_cap + SCAN_TILE - 1) / SCAN_TILE, 8 * sms);
-    out[BK_ONE] = 1;
     out[BK_SSMALL] = clampi(a.cell_cap / 512 + 1, 8 * sms);
     out[BK_SMED] = clampi(a.cell_cap / 2048 + 1, 4 * sms);             // 16 warps a block, one cell a warp
     out[BK_SLARGE] = clampi(a.cell_cap / 16384 + 1, 2 * sms);
@@ -971,7 +928,7 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
 template <bool MULTI>
 static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BatchGrid& g,
                               bool skip_bbox, int bitmap_words, cudaStream_t st) {
-    count_launches(skip_bbox ? 9 : 10);
+    count_launches(skip_bbox ? 8 : 9);
     const int* f[kBuildKinds];
     for (int k = 0; k < kBuildKinds; ++k) f[k] = MULTI ? g.first[k] : nullptr;
     if (!skip_bbox)
@@ -979,7 +936,6 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     launch_k(zero_offsets_kernel<MULTI>, g.total[BK_ZERO], 256, 0, st, one, many, f[BK_ZERO], ntasks);
     launch_k(count_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
     launch_k(scan_reduce_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
-    launch_k(scan_tiles_kernel<MULTI>, g.total[BK_ONE], 1024, 0, st, one, many, f[BK_ONE], ntasks);
     launch_k(scan_down_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
     launch_k(scatter_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
     launch_k(sort_small_kernel<MULTI>, g.total[BK_SSMALL], 256, 0, st, one, many, f[BK_SSMALL], ntasks);

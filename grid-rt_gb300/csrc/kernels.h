@@ -42,7 +42,7 @@ unsigned long long launches_so_far();
 void launch_build(const BuildArgs& a, cudaStream_t st);
 
 // Build kernels by work shape (grid sizing per task).
-enum BuildKind { BK_BBOX = 0, BK_ZERO, BK_TRI, BK_TILE, BK_ONE, BK_SSMALL, BK_SMED, BK_SLARGE, BK_REFS, kBuildKinds };
+enum BuildKind { BK_BBOX = 0, BK_ZERO, BK_TRI, BK_TILE, BK_SSMALL, BK_SMED, BK_SLARGE, BK_REFS, kBuildKinds };
 // Per-task block counts of every build kernel (the single-scene grid sizes).
 void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]);
 // Batch launch: total[k] blocks for kernel kind k, first[k] a device prefix
