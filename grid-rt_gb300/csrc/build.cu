@@ -707,42 +707,63 @@ __global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const Bu
     }
 }
 
-// Cells of 33..256 entries: one warp per cell, bitonic network over a
-// power-of-two pad (64..256) in the warp's own shared-memory slice.
-static constexpr int MED_WARPS = 16;    // warps of a 512-thread block
+// Cells of 33..256 entries: one warp per cell, a bitonic network over a
+// power-of-two pad m = 32 V (V = 2, 4, 8 values per lane) held in registers:
+// element e = 32 r + lane sits in register r of its lane, so strides below 32
+// pair lanes (one shuffle per register) and strides of 32 and above pair
+// registers of the same lane.  Every step is independent across the V
+// registers, so a 256-entry list takes 36 steps of a few pipelined
+// instructions instead of 144 dependent shared-memory round trips.
+template <int V>
+__device__ __forceinline__ void warp_bitonic_regs(int32_t* __restrict__ ids, int32_t s, int32_t n) {
+    const int lane = threadIdx.x & 31;
+    int32_t v[V];
+#pragma unroll
+    for (int r = 0; r < V; ++r) v[r] = 32 * r + lane < n ? ids[s + 32 * r + lane] : INT_MAX;
+#pragma unroll
+    for (int k = 2; k <= 32 * V; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j < 32) {
+#pragma unroll
+                for (int r = 0; r < V; ++r) {
+                    const int32_t o = __shfl_xor_sync(FULL, v[r], j);
+                    const bool up = ((32 * r + lane) & k) == 0;
+                    const bool lower = (lane & j) == 0;
+                    v[r] = (lower == up) ? min(v[r], o) : max(v[r], o);
+                }
+            } else {
+                const int jr = j >> 5;
+#pragma unroll
+                for (int r = 0; r < V; ++r) {
+                    if ((r & jr) == 0) {
+                        const bool up = ((32 * r + lane) & k) == 0;
+                        const int32_t lo = min(v[r], v[r | jr]), hi = max(v[r], v[r | jr]);
+                        v[r] = up ? lo : hi;
+                        v[r | jr] = up ? hi : lo;
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < V; ++r)
+        if (32 * r + lane < n) ids[s + 32 * r + lane] = v[r];
+}
 
 __device__ __forceinline__ void sort_medium_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, const int32_t* __restrict__ q,
                                                           const BuildWork* w, const GridParams* p, unsigned vbx, unsigned vgx) {
     if (sort_skip(p)) return;
-    __shared__ int32_t sh[MED_WARPS][SORT_MED_MAX];
-    const int lane = threadIdx.x & 31;
-    int32_t* a = sh[threadIdx.x >> 5];
     const uint32_t nq = w->nsort[1];
     const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
     for (int64_t i = warp; i < nq; i += nwarps) {
         const int32_t c = q[i];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
-        int m = 64;
-        while (m < n) m <<= 1;
-        for (int t = lane; t < m; t += 32) a[t] = t < n ? ids[s + t] : INT_MAX;
-        __syncwarp();
-        for (int k = 2; k <= m; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                // m/2 compare-exchange pairs: pair r joins t (bit j clear) and t + j
-                for (int r = lane; r < (m >> 1); r += 32) {
-                    const int t = ((r & ~(j - 1)) << 1) | (r & (j - 1));
-                    const int o = t + j;
-                    const bool up = (t & k) == 0;
-                    const int32_t x = a[t], y = a[o];
-                    if ((x > y) == up) { a[t] = y; a[o] = x; }
-                }
-                __syncwarp();
-            }
-        }
-        for (int t = lane; t < n; t += 32) ids[s + t] = a[t];
-        __syncwarp();
+        if (n <= 64) warp_bitonic_regs<2>(ids, s, n);
+        else if (n <= 128) warp_bitonic_regs<4>(ids, s, n);
+        else warp_bitonic_regs<8>(ids, s, n);
     }
 }
 
