@@ -504,6 +504,8 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
     const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ int64_t sh[9];
     __shared__ int64_t shs[33];
+    __shared__ uint32_t wq[SCAN_THREADS / 32][3];   // per warp and class: count, then exclusive prefix
+    __shared__ uint32_t qbase[3];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int64_t tile = vbx; tile < ntiles; tile += vgx) {
         int64_t before = 0;
@@ -547,9 +549,10 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             // segment along x), one atomicOr per touched brick word
             const int32_t nx = p->res[0], ny = p->res[1];
             const int32_t bx = (nx + 3) >> 2, by = (ny + 3) >> 2;
-            int32_t cx = (int32_t)(b % nx);
-            const int64_t rest = b / nx;
-            int32_t cy = (int32_t)(rest % ny), cz = (int32_t)(rest / ny);
+            const int32_t b32 = (int32_t)b;   // < C, which fits int32 (else ST_TOO_BIG)
+            int32_t cx = b32 % nx;
+            const int32_t rest = b32 / nx;
+            int32_t cy = rest % ny, cz = rest / ny;
             int64_t word = -1;
             uint32_t mask = 0u;
             for (int i = 0; i < SCAN_ITEMS && b + i < C; ++i) {
@@ -570,8 +573,9 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             if (mask) atomicOr(&occ[word], mask);
         }
         // cells to sort, by size class: three 10-bit counts packed in one
-        // word (at most 16 per thread, 512 per warp), one warp scan, one
-        // atomicAdd per warp and class
+        // word (at most 16 per thread, 512 per warp), one warp scan, then
+        // the warps' totals scanned per class and one atomicAdd per block
+        // and class
         uint32_t packed = 0u;
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
@@ -583,16 +587,26 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             const uint32_t y = __shfl_up_sync(FULL, incl, o);
             if (lane >= o) incl += y;
         }
-        uint32_t base_s = 0u, base_m = 0u, base_l = 0u;
         if (lane == 31) {
-            if (incl & 1023u) base_s = atomicAdd(&w->nsort[0], incl & 1023u);
-            if ((incl >> 10) & 1023u) base_m = atomicAdd(&w->nsort[1], (incl >> 10) & 1023u);
-            if (incl >> 20) base_l = atomicAdd(&w->nsort[2], incl >> 20);
+            wq[wid][0] = incl & 1023u;
+            wq[wid][1] = (incl >> 10) & 1023u;
+            wq[wid][2] = incl >> 20;
         }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            uint32_t tot = 0u;
+            for (int i = 0; i < SCAN_THREADS / 32; ++i) {
+                const uint32_t t = wq[i][threadIdx.x];
+                wq[i][threadIdx.x] = tot;
+                tot += t;
+            }
+            qbase[threadIdx.x] = tot ? atomicAdd(&w->nsort[threadIdx.x], tot) : 0u;
+        }
+        __syncthreads();
         const uint32_t excl = incl - packed;
-        uint32_t js = __shfl_sync(FULL, base_s, 31) + (excl & 1023u);
-        uint32_t jm = __shfl_sync(FULL, base_m, 31) + ((excl >> 10) & 1023u);
-        uint32_t jl = __shfl_sync(FULL, base_l, 31) + (excl >> 20);
+        uint32_t js = qbase[0] + wq[wid][0] + (excl & 1023u);
+        uint32_t jm = qbase[1] + wq[wid][1] + ((excl >> 10) & 1023u);
+        uint32_t jl = qbase[2] + wq[wid][2] + (excl >> 20);
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             if (b + i < C) {
