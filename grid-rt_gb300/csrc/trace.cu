@@ -28,6 +28,7 @@ namespace gridrt {
 static constexpr unsigned FULL = 0xffffffffu;
 static constexpr int32_t kDeferred = -3;    // Lane::id of a ray handed to the warp-per-ray pass
 static constexpr int32_t kNoHeavy = 0x7fffffff;
+static constexpr int kWideEmptyRun = 8;     // empty cells a deferred ray's group walks per turn
 // A ray is also deferred once its tests would pass kHeavyWorkMult x the
 // heavy-cell threshold in total (0: only long lists defer).
 #ifndef GRIDRT_HEAVY_WORK_MULT
@@ -691,17 +692,29 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
         int32_t b = 0, e = 0;
         float hi = 0.0f;
         if (!done) {
-            if (gl == 0) ++cells;
-            const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
-            if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
-                const int32_t c = L.x + L.y * nx + L.z * nxy;
-                b = __ldg(s.offsets + c);
-                e = __ldg(s.offsets + c + 1);
-                hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-                if (gl == 0) tests += (uint32_t)(e - b);
+            // up to kWideEmptyRun empty cells per turn before a list (as the
+            // one-lane walk does), so empty stretches skip the list and
+            // reduction steps below
+            for (int r = 0; r < kWideEmptyRun; ++r) {
+                if (gl == 0) ++cells;
+                const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+                if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
+                    const int32_t c = L.x + L.y * nx + L.z * nxy;
+                    b = __ldg(s.offsets + c);
+                    e = __ldg(s.offsets + c + 1);
+                    hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+                    if (gl == 0) tests += (uint32_t)(e - b);
+                    break;
+                }
+                if (dda_step(P, L)) {
+                    L.id = -1;
+                    done = true;
+                    break;
+                }
             }
         }
         const unsigned trips = __reduce_max_sync(FULL, (unsigned)((e - b + G - 1) / G));
+        if (trips == 0) continue;   // no group of the warp is at a list this turn
         // two entries per lane and turn, both loaded before either is tested
         for (unsigned it = 0; it < trips; it += 2) {
             const int32_t i0 = b + gl + (int32_t)it * G, i1 = i0 + G;
@@ -746,7 +759,7 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
                 L.id = oid;
             }
         }
-        if (!done) {
+        if (!done && e > b) {   // groups that tested a list this turn
             if (L.best < kFltMax) {
                 if (any && !(L.best < L.tmax)) L.id = -1;
                 done = true;
