@@ -25,7 +25,7 @@ SPACE = {
     "order": ("scanline", "morton8"),
     "empty_run": (2, 4, 8),
     "persistent": (True, False),
-    "heavy_cell": (0, 32, 48),
+    "heavy_cell": (0, 24, 32, 48),
     "heavy_lanes": (16, 32),
     "cell_records": (False, True),
     "refill": (0, 16),
