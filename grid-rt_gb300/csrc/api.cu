@@ -176,6 +176,7 @@ void host_resolve(GridParams& p, int32_t k, int64_t ntris, int64_t cell_cap) {
     p.k = k;
     p.ntris = ntris;
     p.status = st;
+    p.max_list = 0u;
 }
 }  // namespace gridrt
 
@@ -223,9 +224,15 @@ namespace gridrt {
 TraceSlot scene_counter(rtg_scene s) {
     const unsigned slot = __atomic_fetch_add(&s->ctr_seq, 1u, __ATOMIC_RELAXED) % kRayCounters;
     TraceSlot t;
-    t.ctr = s->d_ray_ctr + 4 * (size_t)slot;
+    t.ctr = s->d_ray_ctr + 8 * (size_t)slot;
     t.defer = s->d_defer ? s->d_defer + (size_t)slot * kDeferCap : nullptr;
     t.defer_cap = s->d_defer ? kDeferCap : 0;
+    // the block-per-ray pass is launched for scenes whose last checked build
+    // had a list above kHugeList (the group pass handles such lists anyway)
+    if (s->d_defer && s->hp.max_list > (uint32_t)kHugeList) {
+        t.huge = s->d_defer + (size_t)kRayCounters * kDeferCap + (size_t)slot * kHugeCap;
+        t.huge_cap = kHugeCap;
+    }
     return t;
 }
 }  // namespace gridrt
@@ -295,10 +302,10 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
     if (rc == RTG_OK && cudaMallocHost(&s->h_params, sizeof(GridParams)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "pinned");
     if (rc == RTG_OK && cudaMalloc(&s->d_work, sizeof(BuildWork)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "work");
     if (rc == RTG_OK && cudaMalloc(&s->d_ctr, sizeof(TraceCounters)) != cudaSuccess) rc = fail(RTG_NO_MEMORY, "ctr");
-    if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, 4 * kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
+    if (rc == RTG_OK && cudaMalloc(&s->d_ray_ctr, 8 * kRayCounters * sizeof(unsigned long long)) != cudaSuccess)
         rc = fail(RTG_NO_MEMORY, "ray counters");
     if (rc == RTG_OK && s->tune.heavy_cell > 0 &&
-        cudaMalloc(&s->d_defer, sizeof(int2) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
+        cudaMalloc(&s->d_defer, kDeferAlloc) != cudaSuccess) {
         s->d_defer = nullptr;
         rc = fail(RTG_NO_MEMORY, "deferred-ray queues");
     }
@@ -1120,7 +1127,7 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
             if (value < 0) return fail(RTG_INVALID_PARAM, "heavy-cell threshold must be >= 0");
             if (value > 0 && !s->d_defer) {
                 CUDA_TRY(cudaSetDevice(s->device));
-                if (cudaMalloc(&s->d_defer, sizeof(int2) * (size_t)kRayCounters * kDeferCap) != cudaSuccess) {
+                if (cudaMalloc(&s->d_defer, kDeferAlloc) != cudaSuccess) {
                     s->d_defer = nullptr;
                     return fail(RTG_NO_MEMORY, "deferred-ray queues");
                 }

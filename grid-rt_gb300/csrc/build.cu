@@ -154,6 +154,7 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
     p->nrefs = 0;
     p->ntris = ntris;
     p->status = status;
+    p->max_list = 0u;
     if (status) atomicOr(&w->sticky, status);
 }
 
@@ -514,11 +515,15 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
         const int64_t b = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
         int32_t v[SCAN_ITEMS];
         int64_t s = 0;
+        int32_t vmax = 0;
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             v[i] = (b + i < C) ? counts[b + i] : 0;
             s += v[i];
+            vmax = max(vmax, v[i]);
         }
+        vmax = (int32_t)__reduce_max_sync(FULL, (unsigned)vmax);
+        if (lane == 0 && vmax > 0) atomicMax(&p->max_list, (unsigned)vmax);
         int64_t x = s;
         for (int o = 1; o < 32; o <<= 1) {
             int64_t y = __shfl_up_sync(FULL, x, o);

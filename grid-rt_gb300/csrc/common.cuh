@@ -27,7 +27,7 @@ struct GridParams {
     int64_t nrefs;
     int64_t ntris;
     uint32_t status;
-    uint32_t pad;
+    uint32_t max_list;    // longest cell list of the build (set by the scan)
 };
 
 // status bits written by the build kernels

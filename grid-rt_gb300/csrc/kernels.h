@@ -114,10 +114,15 @@ inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
 // zeroes (ray claims, deferred rays, deferred claims) and the deferred-ray
 // queue; launches that may overlap need distinct slots.
 struct TraceSlot {
-    unsigned long long* ctr;
+    unsigned long long* ctr;   // 8 words: ray claims, deferred rays, deferred claims, huge rays, huge claims
     int2* defer;          // {ray, cell} entries
     int32_t defer_cap;
+    int2* huge = nullptr; // {ray, cell} entries of rays at a list above kHugeList (nullptr: no block pass)
+    int32_t huge_cap = 0;
 };
+// Lists longer than this are tested by a whole block (the block-per-ray pass)
+// when the trace's slot has a huge-list queue.
+static constexpr int32_t kHugeList = 2048;
 
 void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
                           const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st);

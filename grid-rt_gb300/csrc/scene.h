@@ -74,6 +74,9 @@ struct rtg_scene_s {
 namespace gridrt {
 constexpr unsigned kRayCounters = 32;
 constexpr int32_t kDeferCap = 65536;    // deferred rays a launch can queue; more are traced in place
+constexpr int32_t kHugeCap = 8192;      // rays a launch can hand to the block-per-ray pass; more stay in the group pass
+// deferred-ray queues and huge-list queues of all counter slots, one allocation
+constexpr size_t kDeferAlloc = sizeof(int2) * (size_t)kRayCounters * (kDeferCap + kHugeCap);
 // Read-only device view of a built scene (for the trace kernels).
 SceneView scene_view(rtg_scene s);
 // Next per-launch counter slot (and deferred-ray queue) of the scene.

@@ -371,6 +371,8 @@ struct TraceIO {
     int32_t heavy;                 // lists longer than this are deferred (kNoHeavy: never)
     int32_t defer_base;            // added to a deferred ray's index (a batch task's first)
     int32_t refill;                // > 0: lane refill at this many idle lanes (trace_refill)
+    int2* huge;                    // rays at a list above kHugeList, for the block pass (nullptr: none)
+    int32_t huge_cap;
 };
 
 // Loads ray `r` into the lane; false when the ray ends at once (misses the
@@ -683,10 +685,16 @@ __device__ __forceinline__ void resume_at(const SParams& P, Lane& L, int32_t cel
 // Walks the group's ray (state in L, identical on its G lanes) to its end.
 // Every lane of the warp calls it; groups that are done idle through the
 // warp-wide list loop and reductions.
+// With `huge` set, a group whose ray reaches a list above kHugeList queues
+// {ray, cell} for the block-per-ray pass instead (counted there) and returns
+// true: that pass finishes the ray.
 template <int G>
-__device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
-                                          uint32_t& cells, uint32_t& tests) {
+__device__ __forceinline__ bool wide_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
+                                          uint32_t& cells, uint32_t& tests, int2* huge = nullptr,
+                                          int32_t huge_cap = 0, unsigned long long* huge_ctr = nullptr,
+                                          int32_t ray_base = 0) {
     const int gl = threadIdx.x & (G - 1);
+    bool handed = false;
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
     while (__any_sync(FULL, !done)) {
         int32_t b = 0, e = 0;
@@ -703,7 +711,6 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
                     b = __ldg(s.offsets + c);
                     e = __ldg(s.offsets + c + 1);
                     hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-                    if (gl == 0) tests += (uint32_t)(e - b);
                     break;
                 }
                 if (dda_step(P, L)) {
@@ -713,6 +720,25 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
                 }
             }
         }
+        if (huge) {
+            // lists above kHugeList go to the block-per-ray pass (which visits
+            // the cell again), while its queue has room
+            const bool want = !done && e - b > kHugeList;
+            if (__ballot_sync(FULL, want)) {
+                unsigned long long at = 0;
+                if (want && gl == 0) at = atomicAdd(huge_ctr, 1ull);
+                at = __shfl_sync(FULL, at, (int)(threadIdx.x & 31) & ~(G - 1));
+                if (want && at < (unsigned long long)huge_cap) {
+                    if (gl == 0) {
+                        huge[at] = make_int2(L.ray + ray_base, L.x + L.y * nx + L.z * nxy);
+                        --cells;
+                    }
+                    handed = done = true;
+                    b = e = 0;
+                }
+            }
+        }
+        if (gl == 0) tests += (uint32_t)(e - b);
         const unsigned trips = __reduce_max_sync(FULL, (unsigned)((e - b + G - 1) / G));
         if (trips == 0) continue;   // no group of the warp is at a list this turn
         // two entries per lane and turn, both loaded before either is tested
@@ -769,6 +795,7 @@ __device__ __forceinline__ void wide_walk(const SParams& P, const SceneView& s, 
             }
         }
     }
+    return handed;
 }
 
 template <int MODE, bool COUNT, int G>
@@ -801,11 +828,119 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
                 resume_at(P, L, d.y);
             }
         }
-        wide_walk<G>(P, s, L, done, MODE == MODE_ANY, cells, tests);
-        if (valid && gl == 0) finish_ray<MODE>(io, P, s.tris, L);
+        const bool handed =
+            wide_walk<G>(P, s, L, done, MODE == MODE_ANY, cells, tests, io.huge, io.huge_cap, io.counter + 3);
+        if (valid && gl == 0 && !handed) finish_ray<MODE>(io, P, s.tris, L);
     }
     if (COUNT) {
         if (gl != 0) cells = tests = 0;
+        flush_counters(io.ctr, 0, cells, tests);
+    }
+}
+
+// Block-per-ray pass over the rays the group pass met at a list above
+// kHugeList (a dense cluster: tens of thousands of triangles in one cell):
+// all threads of the block hold the ray and step the same DDA; each list is
+// split over the block (thread j tests entries j, j + blockDim, ...), each
+// thread keeping the first minimum of its share, and a block reduction takes
+// the minimum t, ties to the earlier entry -- the one-lane walk's result, as
+// in the group pass.  A ray's walk then takes a block's time per list, not a
+// lane's or a group's.
+static constexpr int kHugeThreads = 256;
+
+template <int MODE, bool COUNT>
+__global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, TraceIO io) {
+    pdl_begin();
+    __shared__ SParams P;
+    __shared__ float red_t[kHugeThreads / 32];
+    __shared__ int32_t red_id[kHugeThreads / 32];
+    __shared__ unsigned long long claim;
+    load_sparams(s.params, P);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long nh = io.counter[3];
+    if (nh > (unsigned long long)io.huge_cap) nh = (unsigned long long)io.huge_cap;
+    uint32_t cells = 0, tests = 0;
+    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
+    for (;;) {
+        if (threadIdx.x == 0) claim = atomicAdd(io.counter + 4, 1ull);
+        __syncthreads();
+        const unsigned long long j = claim;
+        __syncthreads();
+        if (j >= nh) break;
+        const int2 d = __ldg(io.huge + j);
+        Lane L;
+        L.ray = d.x;
+        bool done = !start_ray<MODE>(P, io, L, L.ray);   // the same on every thread
+        if (done) {
+            if (L.id != -2) L.id = -1;
+        } else {
+            resume_at(P, L, d.y);
+        }
+        while (!done) {
+            if (threadIdx.x == 0) ++cells;
+            const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+            if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
+                const int32_t c = L.x + L.y * nx + L.z * nxy;
+                const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
+                const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+                if (threadIdx.x == 0) tests += (uint32_t)(e - b);
+                Lane T = L;
+                T.id = -1;
+                if (s.crec) {
+                    for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
+                        const float4 A = __ldg(s.crec + 3 * (int64_t)i), B = __ldg(s.crec + 3 * (int64_t)i + 1),
+                                     C = __ldg(s.crec + 3 * (int64_t)i + 2);
+                        test_tri<MODE_NEAREST>(T, __float_as_int(A.w), A, B, C, hi);
+                    }
+                } else {
+                    for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
+                        const int32_t t = __ldg(s.ids + i);
+                        const float4 A = __ldg(s.tris + 3 * (int64_t)t), B = __ldg(s.tris + 3 * (int64_t)t + 1),
+                                     C = __ldg(s.tris + 3 * (int64_t)t + 2);
+                        test_tri<MODE_NEAREST>(T, t, A, B, C, hi);
+                    }
+                }
+                // ids ascend along a list: the smaller id is the earlier entry
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ot = __shfl_xor_sync(FULL, T.best, o);
+                    const int32_t oid = __shfl_xor_sync(FULL, T.id, o);
+                    if (ot < T.best || (ot == T.best && (uint32_t)oid < (uint32_t)T.id)) {
+                        T.best = ot;
+                        T.id = oid;
+                    }
+                }
+                if (lane == 0) {
+                    red_t[wid] = T.best;
+                    red_id[wid] = T.id;
+                }
+                __syncthreads();
+                float bt = red_t[0];
+                int32_t bid = red_id[0];
+                for (int i = 1; i < kHugeThreads / 32; ++i)
+                    if (red_t[i] < bt || (red_t[i] == bt && (uint32_t)red_id[i] < (uint32_t)bid)) {
+                        bt = red_t[i];
+                        bid = red_id[i];
+                    }
+                __syncthreads();
+                if (bid >= 0) {
+                    // the first cell with a hit ends the walk; any-hit:
+                    // occluded only below tmax
+                    L.best = bt;
+                    L.id = (MODE == MODE_ANY && !(bt < L.tmax)) ? -1 : bid;
+                    done = true;
+                    continue;
+                }
+            }
+            if (dda_step(P, L)) {
+                L.id = -1;
+                done = true;
+            }
+        }
+        if (threadIdx.x == 0) finish_ray<MODE>(io, P, s.tris, L);
+    }
+    if (COUNT) {
+        if (threadIdx.x != 0) cells = tests = 0;
         flush_counters(io.ctr, 0, cells, tests);
     }
 }
@@ -1175,13 +1310,20 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.defer_cap = defer ? slot.defer_cap : 0;
     io.heavy = defer ? tune.heavy_cell : kNoHeavy;
     io.refill = tune.refill;
-    count_launches(defer ? 2 : 1);
-    cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
+    io.huge = defer ? slot.huge : nullptr;
+    io.huge_cap = io.huge ? slot.huge_cap : 0;
+    count_launches(defer ? (io.huge ? 3 : 2) : 1);
+    cudaMemsetAsync(slot.ctr, 0, 5 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {
         if (io.ctr) launch_wide<MODE, true>(s, io, tune, num_sms, st);
         else launch_wide<MODE, false>(s, io, tune, num_sms, st);
+    }
+    if (io.huge) {
+        // two blocks per SM claim the queued rays
+        if (io.ctr) launch_k(trace_huge_kernel<MODE, true>, (unsigned)(2 * num_sms), kHugeThreads, 0, st, s, io);
+        else launch_k(trace_huge_kernel<MODE, false>, (unsigned)(2 * num_sms), kHugeThreads, 0, st, s, io);
     }
 }
 

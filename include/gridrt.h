@@ -462,7 +462,10 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *   RTG_TUNE_HEAVY_CELL  n > 0: a ray that meets a cell list longer than n is finished by a
  *                        second pass that traces it with a group of lanes (the list split
  *                        over them); default 32, 0 off.  Results are identical either way.
- *                        Costs 16 MB of device memory per scene (deferred-ray queues).
+ *                        A ray that then meets a list above 2,048 entries (a dense cluster)
+ *                        is finished by a third pass, one block of threads per ray, when the
+ *                        scene's last checked build had such a list.
+ *                        Costs 19 MB of device memory per scene (the passes' ray queues).
  *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8, 16, 32 (default)
  *   RTG_TUNE_REFILL      n in 1..32: a warp hands new rays to its idle lanes whenever at least
  *                        n are idle, instead of finishing each batch of 32 rays first (pays on

@@ -224,6 +224,40 @@ def test_heavy_cell_counters_match_oracle(gridlib, oracle):
     assert abs(c["tests"] - int(oc[:, 1].sum())) <= 1e-3 * oc[:, 1].sum()
 
 
+def test_huge_list_block_pass_is_exact(gridlib, oracle):
+    """Lists above 2,048 entries (59,000 triangles in a 0.1^3 cluster, k = 4)
+    go from the group pass to the block-per-ray pass: hit words, frame
+    outputs, occlusion and traversal counters equal the one-lane walk's, and
+    the hits meet the oracle's near-tie rules."""
+    sc = scenes.skewed_density(n=1 << 16)
+    s = _scene(gridlib, sc, 4)      # a synchronous build: the scene knows its longest list
+    g = oracle.Grid(sc.verts, sc.idx, 4)
+    assert int(np.diff(np.asarray(g.offsets)).max()) > 2048
+    cam = scenes.skewed_density_camera(256, 256)
+    rays = scenes.camera_rays(cam, "morton8")
+    rng = np.random.default_rng(3)
+    rays_any = scenes.random_rays(rng, 40_000, (-0.06, -0.06, -0.06), (0.06, 0.06, 0.06))
+    rays_any[:, 7] = 0.05
+    s.set_tuning(heavy_cell=0)
+    s.counters(reset=True)
+    h0 = s.trace_nearest(rays, counters=True)
+    c0 = s.counters(reset=True)
+    o0 = s.trace_any(rays_any)
+    f0 = _frame(s, cam)
+    for lanes in (8, 32):
+        s.set_tuning(heavy_cell=32, heavy_lanes=lanes)
+        h1 = s.trace_nearest(rays, counters=True)
+        c1 = s.counters(reset=True)
+        assert np.array_equal(h0.view(np.int32), h1.view(np.int32)), lanes
+        assert c1 == c0, (c0, c1)
+        assert np.array_equal(o0, s.trace_any(rays_any)), lanes
+        for a, b in zip(f0, _frame(s, cam)):
+            assert np.array_equal(a, b), lanes
+    st = parity.compare_hits(gridlib.split_hits(h0), g.trace_closest(rays), sc.verts, sc.idx, rays, oracle)
+    _report("huge lists", st)
+    parity.assert_parity(st)
+
+
 def test_diffuse_secondary_rays(gridlib, oracle):
     """Skewed-density workload: primary camera rays, then one cosine-weighted
     diffuse ray per hit generated on the device; both generations match the
