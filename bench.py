@@ -640,21 +640,21 @@ def run_batched(args, rank, ws, local, dist):
 
     def measure(cfg):
         b = batch_for(cfg["k"], cfg["order"])
-        b.set_tuning(empty_run=cfg["empty_run"], persistent=True)
+        b.set_tuning(empty_run=cfg["empty_run"], persistent=True, refill=cfg["refill"])
         ms, _ = time_batch(b, 2)
         return ms
 
-    space = {"k": (2, 4, 8), "order": ("scanline", "morton8"), "empty_run": (2, 4, 8)}
+    space = {"k": (2, 4, 8), "order": ("scanline", "morton8"), "empty_run": (2, 4, 8), "refill": (0, 8)}
     best, allres = autotune.search(measure, space=space, reps=1)
     b = batch_for(best["k"], best["order"])
-    b.set_tuning(empty_run=best["empty_run"], persistent=True)
+    b.set_tuning(empty_run=best["empty_run"], persistent=True, refill=best["refill"])
     _barrier(dist)
     batched_ms, graph = time_batch(b, max(3, args.steps // 10))
     batched_ms = _max_over_ranks(batched_ms, dist)
 
     # plain: per scene, synchronous build then one trace launch, in sequence
     for sc in scs:
-        sc.set_tuning(empty_run=best["empty_run"], persistent=True)
+        sc.set_tuning(empty_run=best["empty_run"], persistent=True, refill=best["refill"])
 
     def plain_pass():
         for i, sc in enumerate(scs):
@@ -1066,6 +1066,7 @@ def run_serving(args, rank, ws, local, dist):
         s = lib.Scene(local)
         s.set_geometry(sc.verts, sc.idx)
         s.build(4)
+        s.set_tuning(refill=args.serve_refill)
         inf = s.info()
         scene_bytes += 12 * sc.nverts + 12 * sc.ntris + 48 * sc.ntris + 8 * (inf["ncells"] + 1) + 8 * inf["nrefs"]
         tris += sc.ntris
@@ -1137,6 +1138,7 @@ def run_serving(args, rank, ws, local, dist):
         d_out = torch.empty(n * (1 if mode == lib.RTG_MODE_ANY else 16), dtype=torch.uint8, device=dev)
         tasks.append((si, mode, d_rays, n, d_out))
     ceil_batch = lib.Batch(scs, [4] * nscenes, tasks)
+    ceil_batch.set_tuning(refill=args.serve_refill)
     st = torch.cuda.Stream(device=dev)
     ceil_batch.trace_async(st.cuda_stream)
     torch.cuda.synchronize()
@@ -1161,7 +1163,8 @@ def run_serving(args, rank, ws, local, dist):
         "config": {"workload": "serving_16_scenes", "scenes": nscenes, "triangles": tris,
                    "scene_bytes": int(scene_bytes), "pool_bytes": pool_bytes, "hbm_budget_bytes": budget,
                    "rays_per_request": "log-uniform [1e3, 4e6]", "modes": "70% closest / 30% any-hit",
-                   "max_in_flight": {"served": 3, "plain": 1, "plain_pipelined": 3}},
+                   "max_in_flight": {"served": 3, "plain": 1, "plain_pipelined": 3},
+                   "refill": args.serve_refill},
         "saturation": saturation, "served_over_plain": round(saturation["served"]["mrays_s"] /
                                                               saturation["plain"]["mrays_s"], 3),
         "served_over_plain_pipelined": round(saturation["served"]["mrays_s"] /
@@ -1199,6 +1202,8 @@ def main():
                     choices=["deforming", "batched", "serving", "skewed", "instances", "render"])
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
+    ap.add_argument("--serve-refill", type=int, default=8,
+                    help="lane-refill threshold of the serving scenes (served and plain paths alike)")
     ap.add_argument("--fixed-tuning", default="",
                     help="skip the autotuner: e.g. k=8,order=morton8,empty_run=4,persistent=0 (profiling runs)")
     args = ap.parse_args()

@@ -1096,6 +1096,11 @@ rtg_status rtg_batch_set_tuning(rtg_batch b, int32_t key, int32_t value) {
         b->tune.heavy_lanes = value;
         return RTG_OK;
     }
+    if (key == RTG_TUNE_REFILL) {
+        if (value < 0 || value > 32) return fail(RTG_INVALID_PARAM, "refill threshold must be 0..32");
+        b->tune.refill = value;
+        return RTG_OK;
+    }
     return fail(RTG_INVALID_PARAM, "unknown tuning key");
 }
 

@@ -956,14 +956,102 @@ __device__ __forceinline__ int find_task(const BatchTask* __restrict__ tasks, in
     return lo;
 }
 
+// Lane refill inside one batch task (TraceIO::refill > 0): the warp draws
+// 32-ray chunks from the flattened counter and hands their rays to idle
+// lanes while the chunks belong to its task, so scene and mode stay
+// warp-uniform; a chunk of a later task ends the task here once its rays
+// are finished and is returned (or a value >= total at the end).
+template <int MODE, int ER>
+__device__ __forceinline__ unsigned long long trace_task_refill(const SParams& P, const SceneView& s,
+                                                                const TraceIO& io, Lane& L, long long tfirst,
+                                                                unsigned long long chunk, long long total,
+                                                                uint32_t& cells, uint32_t& tests,
+                                                                uint32_t& started) {
+    const int lane = threadIdx.x & 31;
+    long long pb = (long long)chunk - tfirst;                 // task-local rays not yet started: [pb, pe)
+    long long pe = pb + 32 < io.n ? pb + 32 : io.n;
+    unsigned long long next = ~0ull;                          // a claimed chunk past this task
+    bool active = false;
+    int32_t heavy = io.heavy, work_cap = kNoHeavy;
+    for (;;) {
+        const unsigned idle = __ballot_sync(FULL, !active);
+        const int nidle = __popc(idle);
+        const bool room = nidle >= io.refill || idle == FULL;
+        if (pb >= pe && next == ~0ull && room) {
+            unsigned long long nb = 0;
+            if (lane == 0) nb = atomicAdd(io.counter, 32ull);
+            nb = __shfl_sync(FULL, nb, 0);
+            if ((long long)nb < tfirst + io.n) {
+                pb = (long long)nb - tfirst;
+                pe = pb + 32 < io.n ? pb + 32 : io.n;
+            } else {
+                next = nb;
+            }
+        }
+        if (pb < pe && room) {
+            const int take = (long long)nidle < pe - pb ? nidle : (int)(pe - pb);
+            if (!active) {
+                const int rank = __popc(idle & ((1u << lane) - 1u));
+                if (rank < take) {
+                    L.ray = (int32_t)(pb + rank);
+                    heavy = io.heavy;
+                    work_cap = heavy < kNoHeavy / (kHeavyWorkMult + 1) && kHeavyWorkMult > 0 ? heavy * kHeavyWorkMult
+                                                                                             : kNoHeavy;
+                    ++started;
+                    if (start_ray<MODE>(P, io, L, L.ray)) {
+                        active = true;
+                    } else {
+                        if (L.id != -2) L.id = -1;
+                        finish_ray<MODE>(io, P, s.tris, L);
+                    }
+                }
+            }
+            pb += take;
+        }
+        if (!__any_sync(FULL, active)) {
+            if (pb >= pe && next != ~0ull) return next;
+            continue;
+        }
+        bool fin = active &&
+                   advance<MODE, ER>(P, L, s.offsets, s.ids, s.tris, s.occ, s.crec, heavy, work_cap, cells, tests);
+        if (io.defer) {
+            const bool d = fin && L.id == kDeferred;
+            const unsigned m = __ballot_sync(FULL, d);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                unsigned long long at = 0;
+                if (lane == leader) at = atomicAdd(io.counter + 1, (unsigned long long)__popc(m));
+                at = __shfl_sync(FULL, at, leader);
+                if (d) {
+                    const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
+                    if (slot < (unsigned long long)io.defer_cap) {
+                        io.defer[slot] = make_int2(L.ray + io.defer_base,
+                                                   L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
+                        active = false;
+                    } else {
+                        heavy = kNoHeavy;
+                        work_cap = kNoHeavy;
+                        L.id = -1;
+                    }
+                    fin = false;
+                }
+            }
+        }
+        if (fin) {
+            finish_ray<MODE>(io, P, s.tris, L);
+            active = false;
+        }
+    }
+}
+
 // Many (scene, ray batch) tasks in one persistent launch.  Task t owns the
 // 32-aligned index range [first, first + n) of one flattened ray space, so a
 // 32-ray claim always falls inside one task: scene and mode are warp-uniform.
-template <int ER>
+template <int ER, bool REFILL>
 __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
     trace_batch_kernel(const BatchScene* __restrict__ scenes, int nscenes, const BatchTask* __restrict__ tasks,
                        int ntasks, long long total, unsigned long long* counter, int2* defer, int32_t defer_cap,
-                       int32_t heavy) {
+                       int32_t heavy, int32_t refill) {
     pdl_begin();
     __shared__ SParams P[kMaxBatchScenes];
     for (int i = threadIdx.x; i < nscenes; i += blockDim.x) fill_sparams(scenes[i].view.params, P[i]);
@@ -971,11 +1059,10 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
     const int lane = threadIdx.x & 31;
     Lane L;
     uint32_t cells = 0, tests = 0, started = 0;
-    for (;;) {
-        unsigned long long b = 0;
-        if (lane == 0) b = atomicAdd(counter, 32ull);
-        b = __shfl_sync(FULL, b, 0);
-        if ((long long)b >= total) break;
+    unsigned long long b = 0;
+    if (lane == 0) b = atomicAdd(counter, 32ull);
+    b = __shfl_sync(FULL, b, 0);
+    while ((long long)b < total) {
         const BatchTask T = tasks[find_task(tasks, ntasks, (long long)b)];
         const SceneView V = scenes[T.scene].view;
         TraceIO io{};
@@ -986,6 +1073,18 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
         io.defer_cap = defer_cap;
         io.heavy = defer ? heavy : kNoHeavy;
         io.defer_base = (int32_t)T.first;
+        io.refill = refill;
+        if (REFILL) {
+            if (T.mode == MODE_ANY) {
+                io.occ = static_cast<uint8_t*>(T.out);
+                b = trace_task_refill<MODE_ANY, ER>(P[T.scene], V, io, L, T.first, b, total, cells, tests, started);
+            } else {
+                io.hits = static_cast<int4*>(T.out);
+                b = trace_task_refill<MODE_NEAREST, ER>(P[T.scene], V, io, L, T.first, b, total, cells, tests,
+                                                        started);
+            }
+            continue;
+        }
         const long long base = (long long)b - T.first;
         if (T.mode == MODE_ANY) {
             io.occ = static_cast<uint8_t*>(T.out);
@@ -994,6 +1093,8 @@ __global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS)
             io.hits = static_cast<int4*>(T.out);
             trace_batch32<MODE_NEAREST, ER>(P[T.scene], V, io, L, base, cells, tests, started);
         }
+        if (lane == 0) b = atomicAdd(counter, 32ull);
+        b = __shfl_sync(FULL, b, 0);
     }
 }
 
@@ -1370,18 +1471,22 @@ void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, 
 
 template <int ER>
 static void launch_batch_er(const BatchScene* scenes, int nscenes, const BatchTask* tasks, int ntasks, long long total,
-                            const TraceSlot& slot, int32_t heavy, int num_sms, cudaStream_t st) {
+                            const TraceSlot& slot, int32_t heavy, int32_t refill, int num_sms, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_batch_kernel<ER>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_batch_kernel<ER, false>, 128, 0);
         per_sm = b > 0 ? b : 1;
     }
     long long blocks = (total + 127) / 128;
     blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
     if (blocks < 1) blocks = 1;
-    launch_k(trace_batch_kernel<ER>, (unsigned)blocks, 128, 0, st, scenes, nscenes, tasks, ntasks, total, slot.ctr,
-             heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy);
+    if (refill > 0)
+        launch_k(trace_batch_kernel<ER, true>, (unsigned)blocks, 128, 0, st, scenes, nscenes, tasks, ntasks, total,
+                 slot.ctr, heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy, refill);
+    else
+        launch_k(trace_batch_kernel<ER, false>, (unsigned)blocks, 128, 0, st, scenes, nscenes, tasks, ntasks, total,
+                 slot.ctr, heavy > 0 ? slot.defer : nullptr, slot.defer_cap, heavy, refill);
 }
 
 template <int G>
@@ -1405,10 +1510,10 @@ void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* 
     const int32_t heavy = defer ? tune.heavy_cell : 0;
     count_launches(defer ? 2 : 1);
     cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
-    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
-    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
-    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
-    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, slot, heavy, num_sms, st);
+    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
+    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
+    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
+    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
     if (defer) {
         if (tune.heavy_lanes <= 4) launch_wide_batch<4>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);
         else if (tune.heavy_lanes <= 8) launch_wide_batch<8>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);

@@ -557,7 +557,9 @@ class Batch:
         return r.value
 
     def set_tuning(self, empty_run: int = None, persistent: bool = None, heavy_cell: int = None,
-                   heavy_lanes: int = None):
+                   heavy_lanes: int = None, refill: int = None):
+        if refill is not None:
+            check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_REFILL, int(refill)))
         if heavy_cell is not None:
             check(load().rtg_batch_set_tuning(self.h, RTG_TUNE_HEAVY_CELL, int(heavy_cell)))
         if heavy_lanes is not None:

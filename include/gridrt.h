@@ -279,9 +279,10 @@ rtg_status rtg_batch_trace_async(rtg_batch batch, void* stream);
 rtg_status rtg_batch_check(rtg_batch batch, void* stream);
 /* Total rays over the batch's tasks. */
 rtg_status rtg_batch_rays(rtg_batch batch, int64_t* rays);
-/* Keys RTG_TUNE_EMPTY_RUN, RTG_TUNE_PERSISTENT, RTG_TUNE_HEAVY_CELL and
- * RTG_TUNE_HEAVY_LANES, as for rtg_scene_set_tuning; cell-ordered records are
- * a per-scene setting. */
+/* Keys RTG_TUNE_EMPTY_RUN, RTG_TUNE_PERSISTENT, RTG_TUNE_HEAVY_CELL,
+ * RTG_TUNE_HEAVY_LANES and RTG_TUNE_REFILL, as for rtg_scene_set_tuning (lane
+ * refill stays within one task: a warp's rays share scene and mode);
+ * cell-ordered records are a per-scene setting. */
 rtg_status rtg_batch_set_tuning(rtg_batch batch, int32_t key, int32_t value);
 rtg_status rtg_batch_destroy(rtg_batch batch);
 

@@ -37,12 +37,13 @@ def test_batch_build_equals_scene_builds(gridlib, oracle):
         assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
 
 
-@pytest.mark.parametrize("cell_records,heavy", [(False, 0), (True, 32), (False, 4)])
-def test_batch_trace_equals_scene_traces(gridlib, cell_records, heavy):
+@pytest.mark.parametrize("cell_records,heavy,refill",
+                         [(False, 0, 0), (True, 32, 0), (False, 4, 0), (True, 32, 8), (False, 4, 16), (False, 0, 1)])
+def test_batch_trace_equals_scene_traces(gridlib, cell_records, heavy, refill):
     """Also with cell-ordered records written by the batched build (every
-    other scene) and read by the batched trace, and with the batch's
-    warp-per-ray pass (heavy > 0; heavy = 4 also overflows its queue) against
-    per-scene traces without it."""
+    other scene) and read by the batched trace, with the batch's warp-per-ray
+    pass (heavy > 0; heavy = 4 also overflows its queue), and with lane
+    refill inside each task, against per-scene traces without them."""
     import torch
     items = _items()
     scs, tasks, outs = [], [], []
@@ -66,7 +67,7 @@ def test_batch_trace_equals_scene_traces(gridlib, cell_records, heavy):
             tasks.append((i, gridlib.RTG_MODE_NEAREST, d_rays[i], n, out))
         outs.append(out)
     b = gridlib.Batch(scs, [4] * len(items), tasks)
-    b.set_tuning(heavy_cell=heavy, heavy_lanes=4 if heavy == 4 else 8)
+    b.set_tuning(heavy_cell=heavy, heavy_lanes=4 if heavy == 4 else 8, refill=refill)
     b.build_async()
     b.trace_async()
     assert b.check() == 0
