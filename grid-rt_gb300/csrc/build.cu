@@ -47,6 +47,22 @@ __device__ __forceinline__ int block_task(const int* __restrict__ first, int nta
 // ---------------------------------------------------------------------------
 // Aabb::buildFrom / expandBy (src/rtcore/Aabb.cpp:11-53): min/max per axis.
 // A NaN coordinate never wins a comparison there, so it is skipped here too.
+// The same blocks first clear the whole offsets capacity (the count pass
+// adds into it) and the occupancy bitmap, which needs no grid parameters.
+__device__ __forceinline__ void zero_capacity(int32_t* __restrict__ offsets, uint32_t* __restrict__ occ,
+                                              int64_t cell_cap, unsigned vbx, unsigned vgx) {
+    const int64_t t0 = (int64_t)vbx * blockDim.x + threadIdx.x, nt = (int64_t)vgx * blockDim.x;
+    const int64_t n4 = cell_cap >> 2;
+    for (int64_t i = t0; i < n4; i += nt) {
+        reinterpret_cast<int4*>(offsets)[i] = make_int4(0, 0, 0, 0);
+        if (occ) reinterpret_cast<uint4*>(occ)[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    for (int64_t i = (n4 << 2) + t0; i < cell_cap; i += nt) {
+        offsets[i] = 0;
+        if (occ) occ[i] = 0u;
+    }
+}
+
 __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts, int64_t nverts,
                                                           BuildWork* w, GridParams* p, int32_t k, int64_t ntris,
                                                           int64_t cell_cap, unsigned vbx, unsigned vgx) {
@@ -165,9 +181,12 @@ __global__ void __launch_bounds__(256) bbox_params_kernel(BuildArgs one, const B
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
-        bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+        const unsigned vbx = blockIdx.x - (unsigned)first[t], vgx = (unsigned)(first[t + 1] - first[t]);
+        zero_capacity(a.offsets, a.occ, a.cell_cap, vbx, vgx);
+        bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, vbx, vgx);
     } else {
         const BuildArgs& a = one;
+        zero_capacity(a.offsets, a.occ, a.cell_cap, blockIdx.x, gridDim.x);
         bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, blockIdx.x, gridDim.x);
     }
 }
@@ -955,7 +974,9 @@ __global__ void __launch_bounds__(256) cell_records_kernel(BuildArgs one, const 
 // its grid sizes, the batch launch concatenates them per task.
 void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     auto clampi = [](int64_t v, int64_t hi) { return (int)(v < 1 ? 1 : (v > hi ? hi : v)); };
-    out[BK_BBOX] = clampi((a.nverts + 255) / 256, 2 * sms);
+    // vertices to reduce, and the capacity to clear (4 cells a thread)
+    const int64_t bbox_work = a.nverts > a.cell_cap / 4 ? a.nverts : a.cell_cap / 4;
+    out[BK_BBOX] = clampi((bbox_work + 255) / 256, 4 * sms);
     out[BK_ZERO] = clampi((a.cell_cap / 4 + 255) / 256, 8 * sms);
     out[BK_TRI] = clampi((a.ntris + 255) / 256, 16 * sms);            // one warp per 32 triangles
     out[BK_TILE] = clampi((a.cell_cap + SCAN_TILE - 1) / SCAN_TILE, 8 * sms);
@@ -968,12 +989,15 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
 template <bool MULTI>
 static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BatchGrid& g,
                               bool skip_bbox, int bitmap_words, cudaStream_t st) {
-    count_launches(skip_bbox ? 8 : 9);
+    count_launches(8);
     const int* f[kBuildKinds];
     for (int k = 0; k < kBuildKinds; ++k) f[k] = MULTI ? g.first[k] : nullptr;
+    // the box pass also clears the offsets and the bitmap; host-resolved
+    // parameters skip it and clear them on their own
     if (!skip_bbox)
         launch_k(bbox_params_kernel<MULTI>, g.total[BK_BBOX], 256, 0, st, one, many, f[BK_BBOX], ntasks);
-    launch_k(zero_offsets_kernel<MULTI>, g.total[BK_ZERO], 256, 0, st, one, many, f[BK_ZERO], ntasks);
+    else
+        launch_k(zero_offsets_kernel<MULTI>, g.total[BK_ZERO], 256, 0, st, one, many, f[BK_ZERO], ntasks);
     launch_k(count_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
     launch_k(scan_reduce_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
     launch_k(scan_down_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
