@@ -87,7 +87,7 @@ struct TraceTuning {
     int cell_records = 0;  // 1: the build also writes triangle records in cell-list order
     int heavy_cell = 32;   // > 0: rays meeting a list longer than this finish in a warp-per-ray pass
     int heavy_lanes = 32;  // lanes per deferred ray in that pass: 4, 8, 16 or 32
-    int refill = 8;        // > 0: idle lanes take new rays once this many are idle (0: finish each batch of 32)
+    int refill = 16;       // > 0: idle lanes take new rays once this many are idle (0: finish each batch of 32)
 };
 
 // Kernel launch with programmatic stream serialisation when GRIDRT_PDL is on
