@@ -70,7 +70,7 @@ int64_t ref_capacity(const rtg_scene s) {
 rtg_status ensure_grid_buffers(rtg_scene s, int64_t cells_plus_one, int64_t refs) {
     CUDA_TRY(grow(s->d_offsets, s->cell_cap, cells_plus_one));
     CUDA_TRY(grow(s->d_occ, s->occ_cap, s->cell_cap));
-    CUDA_TRY(grow(s->d_tiles, s->tiles_cap, s->cell_cap / 4096 + 2));
+    CUDA_TRY(grow(s->d_tiles, s->tiles_cap, s->cell_cap / kScanTile + 2));
     CUDA_TRY(grow(s->d_ids, s->ids_cap, refs));
     CUDA_TRY(grow(s->d_scratch, s->scratch_cap, refs));
     if (s->tune.cell_records) CUDA_TRY(grow(s->d_crec, s->crec_cap, 3 * s->ids_cap));

@@ -455,8 +455,9 @@ __global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const Build
 // then each tile scanned from the sum of the tiles before it
 // ---------------------------------------------------------------------------
 static constexpr int SCAN_THREADS = 256;
-static constexpr int SCAN_ITEMS = 16;
-static constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;   // 4096 cells
+static constexpr int SCAN_ITEMS = kScanTile / SCAN_THREADS;  // 4 cells a thread: short chains, many blocks
+static constexpr int SCAN_TILE = kScanTile;
+static_assert(32 * SCAN_ITEMS < 1024, "per-warp sort-queue counts fit 10 bits");
 
 __device__ __forceinline__ int64_t block_sum_i64(int64_t v, int64_t* sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -597,7 +598,7 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             if (mask) atomicOr(&occ[word], mask);
         }
         // cells to sort, by size class: three 10-bit counts packed in one
-        // word (at most 16 per thread, 512 per warp), one warp scan, then
+        // word (at most SCAN_ITEMS per thread, 32 x that per warp), one warp scan, then
         // the warps' totals scanned per class and one atomicAdd per block
         // and class
         uint32_t packed = 0u;

@@ -35,6 +35,9 @@ struct BuildArgs {
     int num_sms;
 };
 
+// Cells per tile of the count scan (tile sums: cell capacity / kScanTile + 2).
+static constexpr int kScanTile = 1024;
+
 // Process-wide count of kernels launched by this library (diagnostics).
 void count_launches(int n);
 unsigned long long launches_so_far();

@@ -42,7 +42,7 @@ constexpr int64_t kMaxCells = int64_t(1) << 24;   // 16,777,216 cells (tile sums
 constexpr size_t kOffParams = 0;
 constexpr size_t kOffWork = 256;
 constexpr size_t kOffTiles = 512;
-constexpr size_t kTileCount = kMaxCells / 4096 + 2;
+constexpr size_t kTileCount = kMaxCells / kScanTile + 2;
 constexpr size_t kOffQSmall = kOffTiles + ((kTileCount * 8 + 255) / 256) * 256;
 constexpr size_t kQSmall = kMaxRefs / 2 + 2;
 constexpr size_t kOffQMed = kOffQSmall + ((kQSmall * 4 + 255) / 256) * 256;
