@@ -106,7 +106,7 @@ void mark_build(rtg_scene s, cudaStream_t st) {
 }
 
 BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
-    BuildArgs a;
+    BuildArgs a{};   // zeroed padding: batches compare argument blocks bytewise
     a.verts = s->d_verts;
     a.nverts = s->nverts;
     a.idx = s->d_idx;
@@ -933,13 +933,12 @@ rtg_status batch_upload_build(rtg_batch b, cudaStream_t st, bool force) {
     // flat batch grids: per kernel kind, the tasks' single-scene block counts back to back
     const int nt = (int)b->h_build.size();
     std::vector<int> first((size_t)kBuildKinds * (nt + 1));
+    std::vector<int> blocks((size_t)nt * kBuildKinds);
+    for (int t = 0; t < nt; ++t) build_blocks(b->h_build[t], b->num_sms, &blocks[(size_t)t * kBuildKinds]);
     for (int k = 0; k < kBuildKinds; ++k) first[(size_t)k * (nt + 1)] = 0;
-    for (int t = 0; t < nt; ++t) {
-        int blocks[kBuildKinds];
-        build_blocks(b->h_build[t], b->num_sms, blocks);
+    for (int t = 0; t < nt; ++t)
         for (int k = 0; k < kBuildKinds; ++k)
-            first[(size_t)k * (nt + 1) + t + 1] = first[(size_t)k * (nt + 1) + t] + blocks[k];
-    }
+            first[(size_t)k * (nt + 1) + t + 1] = first[(size_t)k * (nt + 1) + t] + blocks[(size_t)t * kBuildKinds + k];
     for (int k = 0; k < kBuildKinds; ++k) {
         b->grid.total[k] = first[(size_t)k * (nt + 1) + nt];
         b->grid.first[k] = b->d_first + (size_t)k * (nt + 1);
