@@ -280,5 +280,50 @@ public:
     }
 };
 
+// The same frames in a render loop, the read-back of frame f overlapped with
+// frame f + 1 (rtg_trace_frame_async): begin() enqueues a frame into one of
+// two host buffer pairs and returns its ticket; finish() waits for that
+// frame and exposes its buffers, valid until the frame two later begins, so
+// finish frame f before beginning frame f + 2.  The copies overlap the next
+// frame when the host memory is pinned; with this std::vector storage they
+// are correct but the driver copies them synchronously.
+class GpuFrameStream {
+public:
+    explicit GpuFrameStream(UniformGridAccStruct& acc) : _acc(acc) {}
+
+    rtg_status begin(const rtg_camera& cam, const float light[3], uint64_t* ticket) {
+        const size_t n = (size_t)cam.width * (size_t)cam.height;
+        const int slot = (int)(_begun & 1);
+        _hits[slot].resize(n);
+        _occ[slot].resize(n);
+        const rtg_status rc = rtg_trace_frame_async(_acc.scene(), &cam, light, _hits[slot].data(),
+                                                    _occ[slot].data(), nullptr, ticket);
+        if (rc == RTG_OK) {
+            _ticket[slot] = *ticket;
+            ++_begun;
+        }
+        return rc;
+    }
+
+    rtg_status finish(uint64_t ticket, const std::vector<rtg_hit>** hits, const std::vector<uint8_t>** occluded) {
+        const int slot = (_begun > 0 && _ticket[(_begun - 1) & 1] == ticket) ? (int)((_begun - 1) & 1)
+                                                                             : (int)(_begun & 1);
+        if (_begun == 0 || _ticket[slot] != ticket) return RTG_INVALID_PARAM;
+        const rtg_status rc = rtg_trace_frame_wait(_acc.scene(), ticket);
+        if (rc == RTG_OK) {
+            *hits = &_hits[slot];
+            *occluded = &_occ[slot];
+        }
+        return rc;
+    }
+
+private:
+    UniformGridAccStruct& _acc;
+    std::vector<rtg_hit> _hits[2];
+    std::vector<uint8_t> _occ[2];
+    uint64_t _ticket[2] = {~0ull, ~0ull};
+    uint64_t _begun = 0;
+};
+
 }  // namespace rtp
 }  // namespace gridrt

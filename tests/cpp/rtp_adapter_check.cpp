@@ -2,7 +2,10 @@
 // reference's Context does: build a Geometry through the builder, then trace
 // rays one by one through the virtual per-ray calls and in one batch.
 // Reads rays and geometry from binary files, writes hits for the Python test.
-//   rtp_adapter_check <verts.f32> <tris.i32> <rays.f32> <out_prefix>
+// With a camera file (an rtg_camera followed by the light position, 3
+// float32) it also renders that frame with GpuFrameRenderer and then as a
+// stream of frames through GpuFrameStream, and reports the words that differ.
+//   rtp_adapter_check <verts.f32> <tris.i32> <rays.f32> <out_prefix> [camera.bin]
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -22,7 +25,7 @@ static std::vector<T> load(const char* path) {
 }
 
 int main(int argc, char** argv) {
-    if (argc != 5) return 2;
+    if (argc != 5 && argc != 6) return 2;
     std::vector<float> verts = load<float>(argv[1]);
     std::vector<int32_t> tris = load<int32_t>(argv[2]);
     std::vector<float> rays = load<float>(argv[3]);
@@ -100,7 +103,44 @@ int main(int argc, char** argv) {
     save(".any_single.u8", any_single.data(), any_single.size());
     save(".any_batch.u8", any_batch.data(), any_batch.size());
     save(".inst.f32", inst_hits.data(), inst_hits.size() * 4);
+    long long frame_diff = -1;
+    if (argc == 6) {
+        std::vector<uint8_t> camfile = load<uint8_t>(argv[5]);
+        if (camfile.size() != sizeof(rtg_camera) + 12) return 2;
+        rtg_camera cam;
+        float light[3];
+        std::memcpy(&cam, camfile.data(), sizeof(cam));
+        std::memcpy(light, camfile.data() + sizeof(cam), 12);
+        std::vector<rtg_hit> ref_hits;
+        std::vector<uint8_t> ref_occ;
+        if (rtp::GpuFrameRenderer::render(*acc, cam, light, ref_hits, ref_occ) != RTG_OK) {
+            std::fprintf(stderr, "frame failed: %s\n", rtg_last_error());
+            return 1;
+        }
+        rtp::GpuFrameStream frames(*acc);
+        frame_diff = 0;
+        uint64_t prev = 0, t = 0;
+        const std::vector<rtg_hit>* h = nullptr;
+        const std::vector<uint8_t>* o = nullptr;
+        auto compare = [&]() {
+            for (size_t i = 0; i < ref_hits.size(); ++i) {
+                frame_diff += std::memcmp(&(*h)[i], &ref_hits[i], sizeof(rtg_hit)) != 0;
+                frame_diff += (*o)[i] != ref_occ[i];
+            }
+        };
+        for (int f = 0; f < 4; ++f) {
+            if (frames.begin(cam, light, &t) != RTG_OK) return 1;
+            if (f > 0) {
+                if (frames.finish(prev, &h, &o) != RTG_OK) return 1;
+                compare();
+            }
+            prev = t;
+        }
+        if (frames.finish(prev, &h, &o) != RTG_OK) return 1;
+        compare();
+    }
     rtg_grid_info gi = acc->gridInfo();
-    std::printf("{\"res\": [%d, %d, %d], \"nrefs\": %lld}\n", gi.res[0], gi.res[1], gi.res[2], (long long)gi.nrefs);
+    std::printf("{\"res\": [%d, %d, %d], \"nrefs\": %lld, \"frame_diff\": %lld}\n", gi.res[0], gi.res[1], gi.res[2],
+                (long long)gi.nrefs, frame_diff);
     return 0;
 }

@@ -2,6 +2,7 @@
 UniformGridAccStructBuilder::buildGeometry and traced ray by ray through the
 virtual IAccStruct calls gives exactly the batched results, and those match
 the oracle under the near-tie rules."""
+import json
 import os
 import subprocess
 
@@ -27,8 +28,14 @@ def test_cpp_plugin_mirror(gridlib, oracle, tmp_path):
     sc.verts.astype(np.float32).tofile(p + ".verts")
     sc.idx.astype(np.int32).tofile(p + ".tris")
     rays.astype(np.float32).tofile(p + ".rays")
-    r = subprocess.run([tool, p + ".verts", p + ".tris", p + ".rays", p], capture_output=True, text=True, timeout=300)
+    # a frame, rendered once and then as a stream of frames with overlapped read-back
+    cam = gridlib.camera_struct(scenes.plane_and_debris_camera(64, 48), "morton8")
+    with open(p + ".cam", "wb") as f:
+        f.write(bytes(cam) + np.asarray(scenes.PLANE_LIGHT, np.float32).tobytes())
+    r = subprocess.run([tool, p + ".verts", p + ".tris", p + ".rays", p, p + ".cam"], capture_output=True, text=True,
+                       timeout=300)
     assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout.strip().splitlines()[-1])["frame_diff"] == 0
     single = np.fromfile(p + ".single.f32", np.float32).reshape(-1, 4)
     batch = np.fromfile(p + ".batch.f32", np.float32).reshape(-1, 4)
     assert np.array_equal(single.view(np.uint32), batch.view(np.uint32))
