@@ -777,6 +777,13 @@ rtg_status rtg_trace_camera_diffuse_device(rtg_scene s, const rtg_camera* cam, u
     return RTG_OK;
 }
 
+// GRIDRT_FUSED_FRAME = 1: rtg_trace_frame_device traces each camera ray's
+// shadow ray in the same lane and launch (MODE_FRAME); 0: a camera launch,
+// then an any-hit launch over the shadow-ray slots.  Same results.
+#ifndef GRIDRT_FUSED_FRAME
+#define GRIDRT_FUSED_FRAME 1
+#endif
+
 rtg_status rtg_trace_frame_device(rtg_scene s, const rtg_camera* cam, const float* light_pos, rtg_hit* d_hits,
                                   uint8_t* d_occ, float* d_shadow_rays, void* stream) {
     if (!light_pos || !d_occ || !d_hits) return fail(RTG_INVALID_PARAM, "NULL arguments");
@@ -789,9 +796,20 @@ rtg_status rtg_trace_frame_device(rtg_scene s, const rtg_camera* cam, const floa
         if (rc) return rc;
         d_shadow_rays = reinterpret_cast<float*>(s->d_io);
     }
+    cudaStream_t st = pick(s, stream);
+#if GRIDRT_FUSED_FRAME
+    if (s->hp.ncells != 0) {
+        // one launch (with its deferred passes): each lane traces its camera
+        // ray, then that hit's shadow ray
+        launch_trace_frame(view(s), camera_args(cam), reinterpret_cast<int4*>(d_hits), light_pos,
+                           reinterpret_cast<float4*>(d_shadow_rays), d_occ, nullptr, next_counter(s), s->tune,
+                           s->num_sms, st);
+        CUDA_TRY(cudaGetLastError());
+        return RTG_OK;
+    }
+#endif
     rc = rtg_trace_camera_device(s, cam, d_hits, light_pos, d_shadow_rays, 0, stream);
     if (rc) return rc;
-    cudaStream_t st = pick(s, stream);
     if (s->hp.ncells == 0) {
         CUDA_TRY(cudaMemsetAsync(d_occ, 2, n, st));
         return RTG_OK;

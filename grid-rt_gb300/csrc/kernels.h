@@ -135,6 +135,13 @@ void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, 
                          float4* shadow_rays, TraceCounters* ctr, const TraceSlot& slot,
                          const TraceTuning& tune, int num_sms, cudaStream_t st, int diffuse = 0,
                          unsigned long long seed = 0);
+// Camera rays and, in the same lanes, each hit's shadow ray (MODE_FRAME):
+// hits, shadow-ray slots (also the deferred passes' source of shadow rays)
+// and occlusion, as launch_trace_camera followed by launch_trace_any over the
+// slots.
+void launch_trace_frame(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
+                        float4* shadow_rays, uint8_t* occ, TraceCounters* ctr, const TraceSlot& slot,
+                        const TraceTuning& tune, int num_sms, cudaStream_t st);
 // Batched tracing: up to kMaxBatchScenes scenes, any number of tasks.
 static constexpr int kMaxBatchScenes = 64;
 struct BatchScene {

@@ -40,7 +40,10 @@ static unsigned long long g_launches = 0;
 void count_launches(int n) { __atomic_add_fetch(&g_launches, (unsigned long long)n, __ATOMIC_RELAXED); }
 unsigned long long launches_so_far() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
-enum Mode : int { MODE_NEAREST = 0, MODE_ANY = 1, MODE_CAMERA = 2 };
+// MODE_FRAME: a camera ray, then in the same lane the shadow ray of its hit
+// (any-hit); Lane::tmax is -inf in the camera phase and the shadow ray's
+// tmax after.
+enum Mode : int { MODE_NEAREST = 0, MODE_ANY = 1, MODE_CAMERA = 2, MODE_FRAME = 3 };
 
 struct SParams {
     float bmin[3], bmax[3], cell[3], inv[3];
@@ -213,7 +216,7 @@ __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, 
     if (acc) {
         L.best = t;
         L.id = tid;
-        if (MODE == MODE_ANY && t < L.tmax) return true;
+        if ((MODE == MODE_ANY || MODE == MODE_FRAME) && t < L.tmax) return true;
     }
     return false;
 }
@@ -285,7 +288,7 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
                 // starts from FLT_MAX; an instance walk from the instances
                 // before it).  Any-hit: the first cell with a hit decides --
                 // here not before tmax
-                if (MODE == MODE_ANY) L.id = -1;
+                if (MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax)) L.id = -1;
                 return true;
             }
             if (dda_step(P, L)) {
@@ -380,7 +383,8 @@ struct TraceIO {
 template <int MODE>
 __device__ __forceinline__ bool start_ray(const SParams& P, const TraceIO& io, Lane& L, int32_t r) {
     float tnear, tfar;
-    if (MODE == MODE_CAMERA) {
+    if (MODE == MODE_FRAME) L.tmax = -INFINITY;   // the camera phase
+    if (MODE == MODE_CAMERA || MODE == MODE_FRAME) {
         int32_t px, py;
         ray_pixel(r, io.cam, px, py);
         const float us = fmul(fadd(__int2float_rn(px), 0.5f), io.cam.inv_w);
@@ -405,7 +409,9 @@ __device__ __forceinline__ bool start_ray(const SParams& P, const TraceIO& io, L
     L.id = -1;
     L.best = kFltMax;
     if (P.failed) return false;
-    return setup_ray(P, L, tnear, tfar);
+    const bool ok = setup_ray(P, L, tnear, tfar);
+    if (MODE == MODE_FRAME) L.tmax = -INFINITY;
+    return ok;
 }
 
 // splitmix64 finaliser: counter-based random bits for ray index `i`.
@@ -434,20 +440,22 @@ __device__ __forceinline__ float3 cosine_dir(float nx, float ny, float nz, unsig
     return make_float3(lx * tx + ly * bx + lz * nx, lx * ty + ly * by + lz * ny, lx * tz + ly * bz + lz * nz);
 }
 
-// Writes the lane's result.  Returns true when the lane goes on with a
-// follow-up ray (no mode does so today; the trace loop supports it).
+// Writes the lane's result (when `write`: the lanes of a group or block that
+// share a ray all compute it, one writes).  Returns true when the lane goes
+// on with a follow-up ray: MODE_FRAME's camera phase sets up the hit's shadow
+// ray in the lane, from the same values it writes to the shadow-ray slot.
 template <int MODE>
 __device__ __forceinline__ bool finish_ray(const TraceIO& io, const SParams& P, const float4* __restrict__ tris,
-                                           Lane& L) {
+                                           Lane& L, bool write = true) {
     const int64_t r = L.ray;
-    if (MODE == MODE_ANY) {
-        io.occ[r] = L.id == -2 ? 2 : (L.id >= 0 ? 1 : 0);
+    if (MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax)) {
+        if (write) io.occ[r] = L.id == -2 ? 2 : (L.id >= 0 ? 1 : 0);
         return false;
     }
     int4 h = make_int4(-1, 0, 0, 0);
     if (L.id >= 0) h = refined_hit(tris, L);
-    io.hits[r] = h;
-    if (MODE == MODE_CAMERA) {
+    if (write) io.hits[r] = h;
+    if (MODE == MODE_CAMERA || MODE == MODE_FRAME) {
         float4 sa = make_float4(0.f, 0.f, 0.f, kRayEpsilon), sb = make_float4(0.f, 0.f, 0.f, -1.0f);
         if (L.id >= 0 && io.diffuse) {
             // secondary diffuse ray from the hit point, offset along the
@@ -483,12 +491,35 @@ __device__ __forceinline__ bool finish_ray(const TraceIO& io, const SParams& P, 
                 sb = make_float4(lx, ly, lz, 1.0f);
             }
         }
-        if (io.shadow_rays) {
+        if (io.shadow_rays && write) {
             io.shadow_rays[2 * r] = sa;
             io.shadow_rays[2 * r + 1] = sb;
         }
+        if (MODE == MODE_FRAME) {
+            // the shadow ray as the any-hit pass would load it from the slot
+            if (sb.w < 0.0f) {
+                if (write) io.occ[r] = 2;
+                return false;
+            }
+            L.ox = sa.x; L.oy = sa.y; L.oz = sa.z;
+            L.dx = sb.x; L.dy = sb.y; L.dz = sb.z;
+            L.id = -1;
+            L.best = kFltMax;
+            if (!setup_ray(P, L, sa.w, sb.w)) {
+                if (write) io.occ[r] = 0;
+                return false;
+            }
+            return true;
+        }
     }
     return false;
+}
+
+// Deferred-queue entry of the lane's ray: its index (plus a batch task's
+// first), or -1 - index for a MODE_FRAME shadow ray.
+template <int MODE>
+__device__ __forceinline__ int32_t defer_tag(const Lane& L, const TraceIO& io) {
+    return (MODE == MODE_FRAME && L.tmax > -kFltMax) ? -1 - L.ray : L.ray + io.defer_base;
 }
 
 template <int MODE, int ER>
@@ -524,7 +555,7 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
                     const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
                     if (slot < (unsigned long long)io.defer_cap) {
                         // the walk resumes at this cell in the warp-per-ray pass
-                        io.defer[slot] = make_int2(L.ray + io.defer_base, L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
+                        io.defer[slot] = make_int2(defer_tag<MODE>(L, io), L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
                         active = false;
                     } else {
                         heavy = kNoHeavy;        // queue full: the lane tests the cell itself
@@ -591,7 +622,7 @@ __device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& 
                         active = true;
                     } else {
                         if (L.id != -2) L.id = -1;
-                        finish_ray<MODE>(io, P, s.tris, L);
+                        active = finish_ray<MODE>(io, P, s.tris, L);
                     }
                 }
             }
@@ -613,7 +644,7 @@ __device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& 
                 if (d) {
                     const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
                     if (slot < (unsigned long long)io.defer_cap) {
-                        io.defer[slot] = make_int2(L.ray + io.defer_base,
+                        io.defer[slot] = make_int2(defer_tag<MODE>(L, io),
                                                    L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
                         active = false;
                     } else {
@@ -625,10 +656,7 @@ __device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& 
                 }
             }
         }
-        if (fin) {
-            finish_ray<MODE>(io, P, s.tris, L);
-            active = false;
-        }
+        if (fin) active = finish_ray<MODE>(io, P, s.tris, L);
     }
 }
 
@@ -686,13 +714,13 @@ __device__ __forceinline__ void resume_at(const SParams& P, Lane& L, int32_t cel
 // Every lane of the warp calls it; groups that are done idle through the
 // warp-wide list loop and reductions.
 // With `huge` set, a group whose ray reaches a list above kHugeList queues
-// {ray, cell} for the block-per-ray pass instead (counted there) and returns
-// true: that pass finishes the ray.
+// {huge_tag, cell} for the block-per-ray pass instead (counted there) and
+// returns true: that pass finishes the ray.
 template <int G>
 __device__ __forceinline__ bool wide_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
                                           uint32_t& cells, uint32_t& tests, int2* huge = nullptr,
                                           int32_t huge_cap = 0, unsigned long long* huge_ctr = nullptr,
-                                          int32_t ray_base = 0) {
+                                          int32_t huge_tag = 0) {
     const int gl = threadIdx.x & (G - 1);
     bool handed = false;
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
@@ -730,7 +758,7 @@ __device__ __forceinline__ bool wide_walk(const SParams& P, const SceneView& s, 
                 at = __shfl_sync(FULL, at, (int)(threadIdx.x & 31) & ~(G - 1));
                 if (want && at < (unsigned long long)huge_cap) {
                     if (gl == 0) {
-                        huge[at] = make_int2(L.ray + ray_base, L.x + L.y * nx + L.z * nxy);
+                        huge[at] = make_int2(huge_tag, L.x + L.y * nx + L.z * nxy);
                         --cells;
                     }
                     handed = done = true;
@@ -818,19 +846,32 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
         Lane L;
         L.best = kFltMax;
         L.id = -1;
+        bool shadow = false;      // MODE_FRAME: the entry is a shadow ray (its slot holds it)
         if (valid) {
             const int2 d = __ldg(io.defer + j);
-            L.ray = d.x;
-            done = !start_ray<MODE>(P, io, L, L.ray);
+            shadow = MODE == MODE_FRAME && d.x < 0;
+            L.ray = shadow ? -1 - d.x : d.x;
+            done = shadow ? !start_ray<MODE_ANY>(P, io, L, L.ray) : !start_ray<MODE>(P, io, L, L.ray);
             if (done) {
                 if (L.id != -2) L.id = -1;
             } else {
                 resume_at(P, L, d.y);
             }
         }
-        const bool handed =
-            wide_walk<G>(P, s, L, done, MODE == MODE_ANY, cells, tests, io.huge, io.huge_cap, io.counter + 3);
-        if (valid && gl == 0 && !handed) finish_ray<MODE>(io, P, s.tris, L);
+        const bool handed = wide_walk<G>(P, s, L, done, MODE == MODE_ANY || shadow, cells, tests, io.huge,
+                                         io.huge_cap, io.counter + 3, shadow ? -1 - L.ray : L.ray);
+        if (MODE == MODE_FRAME) {
+            // a camera ray's group goes on with its hit's shadow ray: every
+            // lane sets it up from the hit (one writes the results)
+            bool second = false;
+            if (valid && !handed) second = finish_ray<MODE>(io, P, s.tris, L, gl == 0);
+            bool done2 = !second;
+            const bool handed2 = wide_walk<G>(P, s, L, done2, true, cells, tests, io.huge, io.huge_cap,
+                                              io.counter + 3, -1 - L.ray);
+            if (second && !handed2 && gl == 0) finish_ray<MODE>(io, P, s.tris, L);
+        } else if (valid && gl == 0 && !handed) {
+            finish_ray<MODE>(io, P, s.tris, L);
+        }
     }
     if (COUNT) {
         if (gl != 0) cells = tests = 0;
@@ -868,14 +909,20 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
         __syncthreads();
         if (j >= nh) break;
         const int2 d = __ldg(io.huge + j);
+        const bool shadow = MODE == MODE_FRAME && d.x < 0;   // MODE_FRAME: a shadow ray (in its slot)
         Lane L;
-        L.ray = d.x;
-        bool done = !start_ray<MODE>(P, io, L, L.ray);   // the same on every thread
+        L.ray = shadow ? -1 - d.x : d.x;
+        // the same on every thread
+        bool done = shadow ? !start_ray<MODE_ANY>(P, io, L, L.ray) : !start_ray<MODE>(P, io, L, L.ray);
         if (done) {
             if (L.id != -2) L.id = -1;
         } else {
             resume_at(P, L, d.y);
         }
+        // one walk, or for a MODE_FRAME camera ray two: its own, then from
+        // its start the shadow ray every thread sets up from the hit
+        for (int phase = 0; phase < 2; ++phase) {
+        const bool any = MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax);
         while (!done) {
             if (threadIdx.x == 0) ++cells;
             const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
@@ -927,7 +974,7 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
                     // the first cell with a hit ends the walk; any-hit:
                     // occluded only below tmax
                     L.best = bt;
-                    L.id = (MODE == MODE_ANY && !(bt < L.tmax)) ? -1 : bid;
+                    L.id = (any && !(bt < L.tmax)) ? -1 : bid;
                     done = true;
                     continue;
                 }
@@ -937,7 +984,9 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
                 done = true;
             }
         }
-        if (threadIdx.x == 0) finish_ray<MODE>(io, P, s.tris, L);
+        if (!finish_ray<MODE>(io, P, s.tris, L, threadIdx.x == 0)) break;
+        done = false;
+        }
     }
     if (COUNT) {
         if (threadIdx.x != 0) cells = tests = 0;
@@ -1025,7 +1074,7 @@ __device__ __forceinline__ unsigned long long trace_task_refill(const SParams& P
                 if (d) {
                     const unsigned long long slot = at + __popc(m & ((1u << lane) - 1u));
                     if (slot < (unsigned long long)io.defer_cap) {
-                        io.defer[slot] = make_int2(L.ray + io.defer_base,
+                        io.defer[slot] = make_int2(defer_tag<MODE>(L, io),
                                                    L.x + L.y * P.res[0] + L.z * P.res[0] * P.res[1]);
                         active = false;
                     } else {
@@ -1467,6 +1516,24 @@ void launch_trace_camera(const SceneView& s, const CameraArgs& cam, int4* hits, 
     io.n = n;
     io.ctr = ctr;
     launch_mode<MODE_CAMERA>(s, io, slot, tune, num_sms, st);
+}
+
+void launch_trace_frame(const SceneView& s, const CameraArgs& cam, int4* hits, const float* light,
+                        float4* shadow_rays, uint8_t* occ, TraceCounters* ctr, const TraceSlot& slot,
+                        const TraceTuning& tune, int num_sms, cudaStream_t st) {
+    const int64_t n = (int64_t)cam.width * cam.height;
+    if (n <= 0) return;
+    TraceIO io{};
+    io.rays = shadow_rays;   // the deferred passes load shadow rays from their slots
+    io.hits = hits;
+    io.occ = occ;
+    io.shadow_rays = shadow_rays;
+    io.cam = cam;
+    io.light = make_float3(light[0], light[1], light[2]);
+    io.has_light = 1;
+    io.n = n;
+    io.ctr = ctr;
+    launch_mode<MODE_FRAME>(s, io, slot, tune, num_sms, st);
 }
 
 template <int ER>

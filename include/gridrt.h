@@ -189,11 +189,13 @@ rtg_status rtg_trace_camera_device(rtg_scene scene, const rtg_camera* cam, rtg_h
  * path; it feeds the skewed-density workload's secondary rays. */
 rtg_status rtg_trace_camera_diffuse_device(rtg_scene scene, const rtg_camera* cam, uint64_t seed, rtg_hit* d_hits,
                                            float* d_secondary_rays, int32_t flags, void* stream);
-/* Primary + shadow frame: camera closest hits, then every hit's shadow ray
- * traced with the any-hit rules (two launches).  occluded[i]: 0 lit,
- * 1 shadowed, 2 no shadow ray.  d_shadow_rays (optional, may be NULL: the
- * scene's staging buffer is used) receives the shadow rays as
- * rtg_trace_camera_device writes them. */
+/* Primary + shadow frame: camera closest hits and every hit's shadow ray
+ * traced with the any-hit rules, the shadow ray in the same thread right
+ * after its camera ray (one launch, plus the deferred-ray passes); the same
+ * results as rtg_trace_camera_device followed by rtg_trace_any_device over
+ * the shadow rays.  occluded[i]: 0 lit, 1 shadowed, 2 no shadow ray.
+ * d_shadow_rays (optional, may be NULL: the scene's staging buffer is used)
+ * receives the shadow rays as rtg_trace_camera_device writes them. */
 rtg_status rtg_trace_frame_device(rtg_scene scene, const rtg_camera* cam, const float* light_pos,
                                   rtg_hit* d_hits, uint8_t* d_occluded, float* d_shadow_rays, void* stream);
 

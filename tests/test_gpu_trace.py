@@ -258,6 +258,42 @@ def test_huge_list_block_pass_is_exact(gridlib, oracle):
     parity.assert_parity(st)
 
 
+@pytest.mark.parametrize("case", ["sphere", "cluster"])
+def test_frame_equals_camera_then_any(gridlib, case):
+    """The frame call (each camera ray's shadow ray traced in the same lane,
+    deferred passes included) gives exactly the hits, shadow-ray slots and
+    occlusion of a camera launch followed by an any-hit launch over the
+    slots -- with deferral, lane refill and, for the dense cluster, the
+    block-per-ray pass."""
+    import torch
+    if case == "sphere":
+        sc, k = scenes.deforming_sphere(4), 8
+        cam, light = scenes.deforming_sphere_camera(512, 512), scenes.SPHERE_LIGHT
+    else:
+        sc, k = scenes.skewed_density(n=1 << 16), 4
+        cam, light = scenes.skewed_density_camera(256, 256), (0.3, 1.5, 0.4)
+    s = _scene(gridlib, sc, k)
+    n = cam.width * cam.height
+    for heavy, refill in ((0, 0), (32, 0), (32, 16)):
+        s.set_tuning(heavy_cell=heavy, refill=refill)
+        d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+        d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+        d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+        s.trace_camera_device(cam, d_hits, light, d_sr, order="morton8")
+        s.trace_any_device(d_sr, n, d_occ)
+        torch.cuda.synchronize()
+        ref = (d_hits.cpu().numpy(), d_sr.cpu().numpy().view(np.uint32), d_occ.cpu().numpy())
+        f_hits = torch.empty_like(d_hits)
+        f_sr = torch.empty_like(d_sr)
+        f_occ = torch.empty_like(d_occ)
+        s.trace_frame_device(cam, light, f_hits, f_occ, f_sr, order="morton8")
+        torch.cuda.synchronize()
+        out = (f_hits.cpu().numpy(), f_sr.cpu().numpy().view(np.uint32), f_occ.cpu().numpy())
+        for a, b in zip(ref, out):
+            assert np.array_equal(a, b), (case, heavy, refill)
+        assert (ref[2] != 2).sum() > 0
+
+
 def test_diffuse_secondary_rays(gridlib, oracle):
     """Skewed-density workload: primary camera rays, then one cosine-weighted
     diffuse ray per hit generated on the device; both generations match the
