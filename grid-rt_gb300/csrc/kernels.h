@@ -90,8 +90,15 @@ struct TraceTuning {
     int cell_records = 0;  // 1: the build also writes triangle records in cell-list order
     int heavy_cell = 32;   // > 0: rays meeting a list longer than this finish in a warp-per-ray pass
     int heavy_lanes = 32;  // lanes per deferred ray in that pass: 4, 8, 16 or 32
-    int refill = 16;       // > 0: idle lanes take new rays once this many are idle (0: finish each batch of 32)
+    int refill = -1;       // > 0: idle lanes take new rays once this many are idle (0: finish each batch of 32);
+                           // -1 (default): 16 for rays given as arrays, off for camera and frame traces
 };
+// The refill threshold of a launch over camera-generated rays (camera and
+// frame traces: coherent, and in a frame each lane's shadow ray follows its
+// camera ray, which refill would interleave) or over rays given as arrays.
+inline int refill_for(const TraceTuning& t, int mode_is_camera) {
+    return t.refill >= 0 ? t.refill : (mode_is_camera ? 0 : 16);
+}
 
 // Kernel launch with programmatic stream serialisation when GRIDRT_PDL is on
 // (the kernels call pdl_begin() first), a plain launch otherwise.

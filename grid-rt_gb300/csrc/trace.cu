@@ -1459,7 +1459,7 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.defer = defer ? slot.defer : nullptr;
     io.defer_cap = defer ? slot.defer_cap : 0;
     io.heavy = defer ? tune.heavy_cell : kNoHeavy;
-    io.refill = tune.refill;
+    io.refill = refill_for(tune, MODE == MODE_CAMERA || MODE == MODE_FRAME);
     io.huge = defer ? slot.huge : nullptr;
     io.huge_cap = io.huge ? slot.huge_cap : 0;
     count_launches(defer ? (io.huge ? 3 : 2) : 1);
@@ -1577,10 +1577,10 @@ void launch_trace_batch(const BatchScene* scenes, int nscenes, const BatchTask* 
     const int32_t heavy = defer ? tune.heavy_cell : 0;
     count_launches(defer ? 2 : 1);
     cudaMemsetAsync(slot.ctr, 0, 3 * sizeof(unsigned long long), st);
-    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
-    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
-    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
-    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, slot, heavy, tune.refill, num_sms, st);
+    if (tune.empty_run <= 2) launch_batch_er<2>(scenes, nscenes, tasks, ntasks, total, slot, heavy, refill_for(tune, 0), num_sms, st);
+    else if (tune.empty_run <= 4) launch_batch_er<4>(scenes, nscenes, tasks, ntasks, total, slot, heavy, refill_for(tune, 0), num_sms, st);
+    else if (tune.empty_run <= 8) launch_batch_er<8>(scenes, nscenes, tasks, ntasks, total, slot, heavy, refill_for(tune, 0), num_sms, st);
+    else launch_batch_er<16>(scenes, nscenes, tasks, ntasks, total, slot, heavy, refill_for(tune, 0), num_sms, st);
     if (defer) {
         if (tune.heavy_lanes <= 4) launch_wide_batch<4>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);
         else if (tune.heavy_lanes <= 8) launch_wide_batch<8>(scenes, nscenes, tasks, ntasks, slot, num_sms, st);

@@ -472,9 +472,10 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *   RTG_TUNE_HEAVY_LANES lanes that trace one deferred ray together: 4, 8, 16, 32 (default)
  *   RTG_TUNE_REFILL      n in 1..32: a warp hands new rays to its idle lanes whenever at least
  *                        n are idle, instead of finishing each batch of 32 rays first (pays on
- *                        incoherent rays: +50 to +65% on random in-box rays at 16, neutral on
- *                        camera rays; 8 gains a little more on incoherent rays and costs ~5% on
- *                        camera rays); default 16, 0 off */
+ *                        incoherent rays: +50 to +65% on random in-box rays at 16; 8 gains a
+ *                        little more there and costs ~5% on camera rays); 0 off.  Unset, it is
+ *                        16 for rays given as arrays (nearest, any, batches) and off for camera
+ *                        and frame traces, whose lanes follow a camera ray with its shadow ray */
 enum {
     RTG_TUNE_EMPTY_RUN = 1,
     RTG_TUNE_PERSISTENT = 2,
