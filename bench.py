@@ -421,12 +421,11 @@ def run_gpu(args, rank, ws, local, dist):
     c2 = s.counters(reset=True)
     n_shadow = int((d_sr[:, 7] >= 0).sum().item())
     c = {"rays": c1["rays"] + n_shadow, "cells": c1["cells"] + c2["cells"], "tests": c1["tests"] + c2["tests"]}
-    # per pixel: 16 B hit and 32 B shadow-ray slot written by the camera
-    # launch, the 32 B slot read and 1 B occlusion written by the any-hit
-    # launch; 8 B per visited cell (occupancy word + list bounds), 52 B per
-    # triangle test (4 B id + 48 B record); camera rays are generated, 0 B
-    alg_bytes = (16 + 32 + 32 + 1) * npix + 8 * c["cells"] + 52 * c["tests"]
-    # the frame's two trace launches, averaged (events around the launches alone)
+    # per camera ray a 16 B hit (the ray itself is generated: 0 B); per
+    # shadow ray 24 B in (origin, direction) and 4 B out; 8 B per visited
+    # cell (list bounds), 52 B per triangle test (4 B id + 48 B record)
+    alg_bytes = 16 * npix + (24 + 4) * n_shadow + 8 * c["cells"] + 52 * c["tests"]
+    # the frame's trace launches, averaged (events around the launches alone)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 10
     with torch.cuda.stream(stream):
@@ -470,8 +469,8 @@ def run_gpu(args, rank, ws, local, dist):
         "autotune": {str(kk): v["all"] for kk, v in tuned.items()},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "trace_kernel camera + any, with their warp-per-ray passes when enabled "
-                               "(one frame's trace launches)",
+                     "kernel": "frame trace_kernel (camera rays, then each hit's shadow ray in the same lane) "
+                               "with its deferred-ray pass (one frame's trace launches)",
                      "alg_bytes_per_launch": int(alg_bytes),
                      "kernel_ms": round(kern_s * 1e3, 4), "cells": int(c["cells"]), "tests": int(c["tests"]),
                      "l2": {"peak": round(l2_peak, 1), "frac": round(achieved / l2_peak, 4),
