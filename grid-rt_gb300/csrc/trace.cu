@@ -889,6 +889,75 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
 // lane's or a group's.
 static constexpr int kHugeThreads = 256;
 
+// The block's ray (identical state on every thread) walked to its end:
+// each list split over the block, a block reduction per list.
+__device__ __forceinline__ void block_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
+                                           uint32_t& cells, uint32_t& tests, float* red_t, int32_t* red_id) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
+    while (!done) {
+        if (threadIdx.x == 0) ++cells;
+        const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
+        if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
+            const int32_t c = L.x + L.y * nx + L.z * nxy;
+            const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
+            const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
+            if (threadIdx.x == 0) tests += (uint32_t)(e - b);
+            Lane T = L;
+            T.id = -1;
+            if (s.crec) {
+                for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
+                    const float4 A = __ldg(s.crec + 3 * (int64_t)i), B = __ldg(s.crec + 3 * (int64_t)i + 1),
+                                 C = __ldg(s.crec + 3 * (int64_t)i + 2);
+                    test_tri<MODE_NEAREST>(T, __float_as_int(A.w), A, B, C, hi);
+                }
+            } else {
+                for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
+                    const int32_t t = __ldg(s.ids + i);
+                    const float4 A = __ldg(s.tris + 3 * (int64_t)t), B = __ldg(s.tris + 3 * (int64_t)t + 1),
+                                 C = __ldg(s.tris + 3 * (int64_t)t + 2);
+                    test_tri<MODE_NEAREST>(T, t, A, B, C, hi);
+                }
+            }
+            // ids ascend along a list: the smaller id is the earlier entry
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ot = __shfl_xor_sync(FULL, T.best, o);
+                const int32_t oid = __shfl_xor_sync(FULL, T.id, o);
+                if (ot < T.best || (ot == T.best && (uint32_t)oid < (uint32_t)T.id)) {
+                    T.best = ot;
+                    T.id = oid;
+                }
+            }
+            if (lane == 0) {
+                red_t[wid] = T.best;
+                red_id[wid] = T.id;
+            }
+            __syncthreads();
+            float bt = red_t[0];
+            int32_t bid = red_id[0];
+            for (int i = 1; i < kHugeThreads / 32; ++i)
+                if (red_t[i] < bt || (red_t[i] == bt && (uint32_t)red_id[i] < (uint32_t)bid)) {
+                    bt = red_t[i];
+                    bid = red_id[i];
+                }
+            __syncthreads();
+            if (bid >= 0) {
+                // the first cell with a hit ends the walk; any-hit:
+                // occluded only below tmax
+                L.best = bt;
+                L.id = (any && !(bt < L.tmax)) ? -1 : bid;
+                done = true;
+                continue;
+            }
+        }
+        if (dda_step(P, L)) {
+            L.id = -1;
+            done = true;
+        }
+    }
+}
+
 template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, TraceIO io) {
     pdl_begin();
@@ -897,11 +966,9 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
     __shared__ int32_t red_id[kHugeThreads / 32];
     __shared__ unsigned long long claim;
     load_sparams(s.params, P);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     unsigned long long nh = io.counter[3];
     if (nh > (unsigned long long)io.huge_cap) nh = (unsigned long long)io.huge_cap;
     uint32_t cells = 0, tests = 0;
-    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
     for (;;) {
         if (threadIdx.x == 0) claim = atomicAdd(io.counter + 4, 1ull);
         __syncthreads();
@@ -922,70 +989,10 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
         // one walk, or for a MODE_FRAME camera ray two: its own, then from
         // its start the shadow ray every thread sets up from the hit
         for (int phase = 0; phase < 2; ++phase) {
-        const bool any = MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax);
-        while (!done) {
-            if (threadIdx.x == 0) ++cells;
-            const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
-            if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
-                const int32_t c = L.x + L.y * nx + L.z * nxy;
-                const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
-                const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-                if (threadIdx.x == 0) tests += (uint32_t)(e - b);
-                Lane T = L;
-                T.id = -1;
-                if (s.crec) {
-                    for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
-                        const float4 A = __ldg(s.crec + 3 * (int64_t)i), B = __ldg(s.crec + 3 * (int64_t)i + 1),
-                                     C = __ldg(s.crec + 3 * (int64_t)i + 2);
-                        test_tri<MODE_NEAREST>(T, __float_as_int(A.w), A, B, C, hi);
-                    }
-                } else {
-                    for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
-                        const int32_t t = __ldg(s.ids + i);
-                        const float4 A = __ldg(s.tris + 3 * (int64_t)t), B = __ldg(s.tris + 3 * (int64_t)t + 1),
-                                     C = __ldg(s.tris + 3 * (int64_t)t + 2);
-                        test_tri<MODE_NEAREST>(T, t, A, B, C, hi);
-                    }
-                }
-                // ids ascend along a list: the smaller id is the earlier entry
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float ot = __shfl_xor_sync(FULL, T.best, o);
-                    const int32_t oid = __shfl_xor_sync(FULL, T.id, o);
-                    if (ot < T.best || (ot == T.best && (uint32_t)oid < (uint32_t)T.id)) {
-                        T.best = ot;
-                        T.id = oid;
-                    }
-                }
-                if (lane == 0) {
-                    red_t[wid] = T.best;
-                    red_id[wid] = T.id;
-                }
-                __syncthreads();
-                float bt = red_t[0];
-                int32_t bid = red_id[0];
-                for (int i = 1; i < kHugeThreads / 32; ++i)
-                    if (red_t[i] < bt || (red_t[i] == bt && (uint32_t)red_id[i] < (uint32_t)bid)) {
-                        bt = red_t[i];
-                        bid = red_id[i];
-                    }
-                __syncthreads();
-                if (bid >= 0) {
-                    // the first cell with a hit ends the walk; any-hit:
-                    // occluded only below tmax
-                    L.best = bt;
-                    L.id = (any && !(bt < L.tmax)) ? -1 : bid;
-                    done = true;
-                    continue;
-                }
-            }
-            if (dda_step(P, L)) {
-                L.id = -1;
-                done = true;
-            }
-        }
-        if (!finish_ray<MODE>(io, P, s.tris, L, threadIdx.x == 0)) break;
-        done = false;
+            block_walk(P, s, L, done, MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax), cells, tests,
+                       red_t, red_id);
+            if (!finish_ray<MODE>(io, P, s.tris, L, threadIdx.x == 0)) break;
+            done = false;
         }
     }
     if (COUNT) {
