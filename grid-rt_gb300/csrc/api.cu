@@ -200,7 +200,7 @@ rtg_status enqueue_build(rtg_scene s, int32_t k, bool skip_bbox, cudaStream_t st
     if (skip_bbox)
         CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(s->d_work) + offsetof(BuildWork, nsort), 0,
                                  sizeof(uint32_t) * 3, st));
-    launch_build(make_args(s, k, skip_bbox), st);
+    launch_build(make_args(s, k, skip_bbox), st, s->have_fork ? &s->fork : nullptr);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;
 }
@@ -310,6 +310,16 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
         rc = fail(RTG_NO_MEMORY, "deferred-ray queues");
     }
     if (rc == RTG_OK) {
+        // the sorts' side streams; without them the build stays on one stream
+        bool ok = cudaStreamCreateWithFlags(&s->fork.side[0], cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaStreamCreateWithFlags(&s->fork.side[1], cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&s->fork.fork, cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&s->fork.join[0], cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&s->fork.join[1], cudaEventDisableTiming) == cudaSuccess;
+        s->have_fork = ok;
+        if (!ok) cudaGetLastError();
+    }
+    if (rc == RTG_OK) {
         BuildWork w;
         std::memset(&w, 0, sizeof(w));
         for (int d = 0; d < 3; ++d) { w.keys[d] = 0xffffffffu; w.keys[3 + d] = 0u; }
@@ -351,6 +361,14 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
     cudaFree(s->d_ctr);
     cudaFree(s->d_verts_back);
     if (s->copy_stream) cudaStreamSynchronize(s->copy_stream);
+    for (int i = 0; i < 2; ++i) {
+        if (s->fork.side[i]) {
+            cudaStreamSynchronize(s->fork.side[i]);
+            cudaStreamDestroy(s->fork.side[i]);
+        }
+        if (s->fork.join[i]) cudaEventDestroy(s->fork.join[i]);
+    }
+    if (s->fork.fork) cudaEventDestroy(s->fork.fork);
     cudaFree(s->d_fring);
     for (int i = 0; i < 2; ++i) {
         if (s->frame_traced[i]) cudaEventDestroy(s->frame_traced[i]);

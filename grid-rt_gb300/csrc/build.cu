@@ -989,7 +989,7 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
 
 template <bool MULTI>
 static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BatchGrid& g,
-                              bool skip_bbox, int bitmap_words, cudaStream_t st) {
+                              bool skip_bbox, int bitmap_words, cudaStream_t st, const BuildFork* fork = nullptr) {
     count_launches(8);
     const int* f[kBuildKinds];
     for (int k = 0; k < kBuildKinds; ++k) f[k] = MULTI ? g.first[k] : nullptr;
@@ -1003,20 +1003,36 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     launch_k(scan_reduce_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
     launch_k(scan_down_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
     launch_k(scatter_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
+    // the three size classes sort disjoint cells: with side streams they run
+    // side by side, joined before the records pass reads the lists
+    cudaStream_t sm = st, sl = st;
+    if (fork) {
+        cudaEventRecord(fork->fork, st);
+        cudaStreamWaitEvent(fork->side[0], fork->fork, 0);
+        cudaStreamWaitEvent(fork->side[1], fork->fork, 0);
+        sm = fork->side[0];
+        sl = fork->side[1];
+    }
     launch_k(sort_small_kernel<MULTI>, g.total[BK_SSMALL], 256, 0, st, one, many, f[BK_SSMALL], ntasks);
-    launch_k(sort_medium_kernel<MULTI>, g.total[BK_SMED], 512, 0, st, one, many, f[BK_SMED], ntasks);
-    launch_k(sort_large_kernel<MULTI>, g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, st, one, many,
+    launch_k(sort_medium_kernel<MULTI>, g.total[BK_SMED], 512, 0, sm, one, many, f[BK_SMED], ntasks);
+    launch_k(sort_large_kernel<MULTI>, g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, sl, one, many,
              f[BK_SLARGE], ntasks);
+    if (fork) {
+        cudaEventRecord(fork->join[0], sm);
+        cudaEventRecord(fork->join[1], sl);
+        cudaStreamWaitEvent(st, fork->join[0], 0);
+        cudaStreamWaitEvent(st, fork->join[1], 0);
+    }
     if (g.total[BK_REFS] > 0) {
         count_launches(1);
         launch_k(cell_records_kernel<MULTI>, g.total[BK_REFS], 256, 0, st, one, many, f[BK_REFS], ntasks);
     }
 }
 
-void launch_build(const BuildArgs& a, cudaStream_t st) {
+void launch_build(const BuildArgs& a, cudaStream_t st, const BuildFork* fork) {
     BatchGrid g{};
     build_blocks(a, a.num_sms, g.total);
-    launch_build_impl<false>(a, nullptr, 1, g, a.skip_bbox, a.bitmap_words, st);
+    launch_build_impl<false>(a, nullptr, 1, g, a.skip_bbox, a.bitmap_words, st, fork);
 }
 
 void launch_build_batch(const BuildArgs* d_tasks, int ntasks, const BatchGrid& g, int bitmap_words,

@@ -42,7 +42,14 @@ static constexpr int kScanTile = 1024;
 void count_launches(int n);
 unsigned long long launches_so_far();
 
-void launch_build(const BuildArgs& a, cudaStream_t st);
+// Side streams and events on which a build runs its three per-cell sorts
+// side by side (they touch disjoint cells); nullptr: one after the other.
+struct BuildFork {
+    cudaStream_t side[2];
+    cudaEvent_t fork;
+    cudaEvent_t join[2];
+};
+void launch_build(const BuildArgs& a, cudaStream_t st, const BuildFork* fork = nullptr);
 
 // Build kernels by work shape (grid sizing per task).
 enum BuildKind { BK_BBOX = 0, BK_ZERO, BK_TRI, BK_TILE, BK_SSMALL, BK_SMED, BK_SLARGE, BK_REFS, kBuildKinds };

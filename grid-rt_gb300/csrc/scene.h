@@ -68,6 +68,9 @@ struct rtg_scene_s {
     cudaEvent_t frame_traced[2] = {nullptr, nullptr};
     cudaEvent_t frame_copied[2] = {nullptr, nullptr};
     uint64_t frame_seq = 0;              // frames enqueued so far
+    // side streams of the build's per-cell sorts (created with the scene)
+    gridrt::BuildFork fork{};
+    bool have_fork = false;
     gridrt::TraceCounters* d_ctr = nullptr;
 };
 
