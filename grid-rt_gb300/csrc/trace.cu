@@ -16,10 +16,14 @@
 // Execution: persistent warps.  A warp claims 32 consecutive rays with one
 // global atomicAdd, traces them to the end (one ray per lane; consecutive
 // camera rays in Morton order stay coherent) and claims the next 32, so no
-// warp idles while a block-mate finishes.  Per loop iteration a lane walks up
-// to ER empty cells (a tuning parameter), decided from a 4x4x2-brick occupancy bitmap whose
-// current word stays in a register, and tests at most one non-empty cell, so
-// lanes that reach triangles test them together.
+// warp idles while a block-mate finishes (or, with lane refill, hands new
+// rays to its idle lanes as it goes).  Per loop iteration a lane walks up to
+// ER empty cells (a tuning parameter), decided from a 4x4x2-brick occupancy
+// bitmap whose current word stays in a register, and tests at most one
+// non-empty cell, so lanes that reach triangles test them together.  A frame
+// (MODE_FRAME) traces each camera ray's shadow ray in the same lane right
+// after it.  Rays that meet a long list finish in a group-of-lanes pass,
+// those that then meet a dense cluster's list in a block-per-ray pass.
 #include "common.cuh"
 #include "kernels.h"
 
