@@ -199,7 +199,7 @@ rtg_status read_clear_sticky(rtg_scene s, uint32_t* out) {
 rtg_status enqueue_build(rtg_scene s, int32_t k, bool skip_bbox, cudaStream_t st) {
     if (skip_bbox)
         CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(s->d_work) + offsetof(BuildWork, nsort), 0,
-                                 sizeof(uint32_t) * 3, st));
+                                 sizeof(BuildWork::nsort), st));
     launch_build(make_args(s, k, skip_bbox), st, s->have_fork ? &s->fork : nullptr);
     CUDA_TRY(cudaGetLastError());
     return RTG_OK;

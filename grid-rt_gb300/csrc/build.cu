@@ -125,7 +125,7 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
         w->keys[3 + d] = 0u;
     }
     w->ticket = 0u;
-    w->nsort[0] = w->nsort[1] = w->nsort[2] = 0u;
+    w->nsort[0] = w->nsort[1] = w->nsort[2] = w->nsort[3] = 0u;
     // Aabb::scaleBy(0.01f) with planar tolerance 0.01f (src/rtcore/Aabb.cpp:78-91)
     for (int d = 0; d < 3; ++d) {
         const float s = (mn[d] == mx[d]) ? 0.01f : fmul(vabs(fsub(mx[d], mn[d])), 0.01f);
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(BuildArgs one, const Build
 static constexpr int SCAN_THREADS = 256;
 static constexpr int SCAN_ITEMS = kScanTile / SCAN_THREADS;  // 4 cells a thread: short chains, many blocks
 static constexpr int SCAN_TILE = kScanTile;
-static_assert(32 * SCAN_ITEMS < 1024, "per-warp sort-queue counts fit 10 bits");
+static_assert(32 * SCAN_ITEMS < 256, "per-warp sort-queue counts fit 8 bits");
 
 __device__ __forceinline__ int64_t block_sum_i64(int64_t v, int64_t* sh) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -507,6 +507,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(BuildArgs one
     }
 }
 
+// Sort-queue class of a cell of n >= 2 entries (its BuildWork::nsort index).
+__device__ __forceinline__ int sort_class(int32_t n) {
+    return n <= SORT_TINY_MAX ? 0 : (n <= SORT_SMALL_MAX ? 3 : (n <= SORT_MED_MAX ? 1 : 2));
+}
+
 // In-place inclusive scan of each tile plus the sum of the tiles before it
 // (each block adds those tile sums itself); queues cells that hold two or
 // more triangles for the segmented sort.  The block of the last tile writes
@@ -525,8 +530,8 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
     const int64_t ntiles = (C + SCAN_TILE - 1) / SCAN_TILE;
     __shared__ int64_t sh[9];
     __shared__ int64_t shs[33];
-    __shared__ uint32_t wq[SCAN_THREADS / 32][3];   // per warp and class: count, then exclusive prefix
-    __shared__ uint32_t qbase[3];
+    __shared__ uint32_t wq[SCAN_THREADS / 32][4];   // per warp and class: count, then exclusive prefix
+    __shared__ uint32_t qbase[4];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int64_t tile = vbx; tile < ntiles; tile += vgx) {
         int64_t before = 0;
@@ -597,15 +602,19 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             }
             if (mask) atomicOr(&occ[word], mask);
         }
-        // cells to sort, by size class: three 10-bit counts packed in one
-        // word (at most SCAN_ITEMS per thread, 32 x that per warp), one warp scan, then
-        // the warps' totals scanned per class and one atomicAdd per block
-        // and class
+        // cells to sort, by size class (the nsort index): four 8-bit counts
+        // packed in one word (at most SCAN_ITEMS per thread, 32 x that per
+        // warp), one warp scan, then the warps' totals scanned per class and
+        // one atomicAdd per block and class.  Cells of 2..8 entries fill the
+        // small queue from the front, cells of 9..32 from the back: a cell
+        // in either holds two or more references, so together they number at
+        // most R / 2 <= ref_cap / 2 < q_small_cap whenever R fits (R above
+        // ref_cap raises ST_REF_CAP and the sorts skip the build)
         uint32_t packed = 0u;
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             const int32_t n = v[i];
-            if (b + i < C && n >= 2) packed += n <= SORT_SMALL_MAX ? 1u : (n <= SORT_MED_MAX ? (1u << 10) : (1u << 20));
+            if (b + i < C && n >= 2) packed += 1u << (8 * sort_class(n));
         }
         uint32_t incl = packed;
         for (int o = 1; o < 32; o <<= 1) {
@@ -613,12 +622,11 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
             if (lane >= o) incl += y;
         }
         if (lane == 31) {
-            wq[wid][0] = incl & 1023u;
-            wq[wid][1] = (incl >> 10) & 1023u;
-            wq[wid][2] = incl >> 20;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) wq[wid][k] = (incl >> (8 * k)) & 255u;
         }
         __syncthreads();
-        if (threadIdx.x < 3) {
+        if (threadIdx.x < 4) {
             uint32_t tot = 0u;
             for (int i = 0; i < SCAN_THREADS / 32; ++i) {
                 const uint32_t t = wq[i][threadIdx.x];
@@ -629,9 +637,10 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
         }
         __syncthreads();
         const uint32_t excl = incl - packed;
-        uint32_t js = qbase[0] + wq[wid][0] + (excl & 1023u);
-        uint32_t jm = qbase[1] + wq[wid][1] + ((excl >> 10) & 1023u);
-        uint32_t jl = qbase[2] + wq[wid][2] + (excl >> 20);
+        uint32_t js = qbase[0] + wq[wid][0] + (excl & 255u);
+        uint32_t jm = qbase[1] + wq[wid][1] + ((excl >> 8) & 255u);
+        uint32_t jl = qbase[2] + wq[wid][2] + ((excl >> 16) & 255u);
+        uint32_t jw = qbase[3] + wq[wid][3] + (excl >> 24);
 #pragma unroll
         for (int i = 0; i < SCAN_ITEMS; ++i) {
             if (b + i < C) {
@@ -639,10 +648,14 @@ __device__ __forceinline__ void scan_down_body(int32_t* __restrict__ counts, Gri
                 counts[b + i] = (int32_t)run;
                 const int32_t n = v[i];
                 if (n >= 2) {
-                    if (n <= SORT_SMALL_MAX) {
+                    if (n <= SORT_TINY_MAX) {
                         if (js < q_small_cap) q_small[js] = (int32_t)(b + i);
                         else raise_status(p, w, ST_SORT_CAP);
                         ++js;
+                    } else if (n <= SORT_SMALL_MAX) {
+                        if (jw < q_small_cap) q_small[q_small_cap - 1 - jw] = (int32_t)(b + i);
+                        else raise_status(p, w, ST_SORT_CAP);
+                        ++jw;
                     } else if (n <= SORT_MED_MAX) {
                         if (jm < q_med_cap) q_med[jm] = (int32_t)(b + i);
                         else raise_status(p, w, ST_SORT_CAP);
@@ -680,55 +693,52 @@ static __device__ __forceinline__ bool sort_skip(const GridParams* p) {
 }
 
 __device__ __forceinline__ void sort_small_body(const int32_t* __restrict__ offsets, int32_t* __restrict__ ids,
-                                                         const int32_t* __restrict__ q, const BuildWork* w,
-                                                         const GridParams* p, unsigned vbx, unsigned vgx) {
+                                                const int32_t* __restrict__ q, int64_t q_cap, const BuildWork* w,
+                                                const GridParams* p, unsigned vbx, unsigned vgx) {
     if (sort_skip(p)) return;
-    const uint32_t nq = w->nsort[0];
     const int lane = threadIdx.x & 31;
-    const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
-    // cells of at most 8 entries: one per thread, a 19-comparator network in
-    // registers; then cells of 9..32 entries: one per warp, a bitonic
-    // network over the lanes
+    // cells of 2..8 entries (the queue's front): one per thread, a
+    // 19-comparator network in registers
+    const uint32_t nt = w->nsort[0];
     const int64_t tid = (int64_t)vbx * blockDim.x + threadIdx.x;
     const int64_t nthreads = (int64_t)vgx * blockDim.x;
-    for (int64_t i = tid; i < nq; i += nthreads) {
+    for (int64_t i = tid; i < nt; i += nthreads) {
         const int32_t c = q[i];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
-        if (n <= 8) {
-            int32_t v[8];
+        int32_t v[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = k < n ? ids[s + k] : INT_MAX;
+        for (int k = 0; k < 8; ++k) v[k] = k < n ? ids[s + k] : INT_MAX;
 #define GRIDRT_CX(a, b) { const int32_t lo_ = min(v[a], v[b]), hi_ = max(v[a], v[b]); v[a] = lo_; v[b] = hi_; }
-            GRIDRT_CX(0, 2) GRIDRT_CX(1, 3) GRIDRT_CX(4, 6) GRIDRT_CX(5, 7)
-            GRIDRT_CX(0, 4) GRIDRT_CX(1, 5) GRIDRT_CX(2, 6) GRIDRT_CX(3, 7)
-            GRIDRT_CX(0, 1) GRIDRT_CX(2, 3) GRIDRT_CX(4, 5) GRIDRT_CX(6, 7)
-            GRIDRT_CX(2, 4) GRIDRT_CX(3, 5)
-            GRIDRT_CX(1, 4) GRIDRT_CX(3, 6)
-            GRIDRT_CX(1, 2) GRIDRT_CX(3, 4) GRIDRT_CX(5, 6)
+        GRIDRT_CX(0, 2) GRIDRT_CX(1, 3) GRIDRT_CX(4, 6) GRIDRT_CX(5, 7)
+        GRIDRT_CX(0, 4) GRIDRT_CX(1, 5) GRIDRT_CX(2, 6) GRIDRT_CX(3, 7)
+        GRIDRT_CX(0, 1) GRIDRT_CX(2, 3) GRIDRT_CX(4, 5) GRIDRT_CX(6, 7)
+        GRIDRT_CX(2, 4) GRIDRT_CX(3, 5)
+        GRIDRT_CX(1, 4) GRIDRT_CX(3, 6)
+        GRIDRT_CX(1, 2) GRIDRT_CX(3, 4) GRIDRT_CX(5, 6)
 #undef GRIDRT_CX
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (k < n) ids[s + k] = v[k];
-        }
+        for (int k = 0; k < 8; ++k)
+            if (k < n) ids[s + k] = v[k];
     }
-    for (int64_t i = warp; i < nq; i += nwarps) {
-        const int32_t c = q[i];
+    // cells of 9..32 entries (the queue's back): one per warp, a bitonic
+    // network over the lanes
+    const uint32_t nw = w->nsort[3];
+    const int64_t warp = tid >> 5, nwarps = nthreads >> 5;
+    for (int64_t i = warp; i < nw; i += nwarps) {
+        const int32_t c = q[q_cap - 1 - i];
         const int32_t cs = offsets[c], cn = offsets[c + 1] - cs;
-        if (cn > 8) {
-            int32_t v = lane < cn ? ids[cs + lane] : INT_MAX;
+        int32_t v = lane < cn ? ids[cs + lane] : INT_MAX;
 #pragma unroll
-            for (int k = 2; k <= 32; k <<= 1) {
+        for (int k = 2; k <= 32; k <<= 1) {
 #pragma unroll
-                for (int j = k >> 1; j > 0; j >>= 1) {
-                    const int32_t o = __shfl_xor_sync(FULL, v, j);
-                    const bool up = (lane & k) == 0;
-                    const bool lower = (lane & j) == 0;
-                    v = (lower == up) ? min(v, o) : max(v, o);
-                }
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                const int32_t o = __shfl_xor_sync(FULL, v, j);
+                const bool up = (lane & k) == 0;
+                const bool lower = (lane & j) == 0;
+                v = (lower == up) ? min(v, o) : max(v, o);
             }
-            if (lane < cn) ids[cs + lane] = v;
         }
+        if (lane < cn) ids[cs + lane] = v;
     }
 }
 
@@ -739,10 +749,10 @@ __global__ void __launch_bounds__(256) sort_small_kernel(BuildArgs one, const Bu
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
-        sort_small_body(a.offsets, a.ids, a.q_small, a.work, a.params, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+        sort_small_body(a.offsets, a.ids, a.q_small, a.q_small_cap, a.work, a.params, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
     } else {
         const BuildArgs& a = one;
-        sort_small_body(a.offsets, a.ids, a.q_small, a.work, a.params, blockIdx.x, gridDim.x);
+        sort_small_body(a.offsets, a.ids, a.q_small, a.q_small_cap, a.work, a.params, blockIdx.x, gridDim.x);
     }
 }
 

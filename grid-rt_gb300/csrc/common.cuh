@@ -58,9 +58,10 @@ __device__ __forceinline__ void pdl_begin() {
 #endif
 }
 
-// Per-cell sort size classes: warp registers up to 32 entries, one warp's
-// shared-memory slice up to 256, a block above (bitonic up to 4096, bitmap
-// beyond).
+// Per-cell sort size classes: one thread's registers up to 8 entries, warp
+// registers up to 32, one warp's registers up to 256, a block above (bitonic
+// up to 4096, bitmap beyond).
+static constexpr int SORT_TINY_MAX = 8;
 static constexpr int SORT_SMALL_MAX = 32;
 static constexpr int SORT_MED_MAX = 256;
 static constexpr int SORT_BLOCK_MAX = 4096;
@@ -69,9 +70,10 @@ static constexpr int SORT_BLOCK_MAX = 4096;
 struct BuildWork {
     uint32_t keys[6];        // ordered-int min xyz, max xyz
     uint32_t ticket;         // last-block ticket of the bbox kernel
-    uint32_t nsort[3];       // cells queued for small / medium / large sorts
+    uint32_t nsort[4];       // cells queued: 2..8 entries (front of the small queue), 33..256, above 256,
+                             // 9..32 (back of the small queue)
     uint32_t sticky;         // OR of every build's status since the host last cleared it
-    uint32_t pad[5];
+    uint32_t pad[4];
 };
 
 static constexpr float kHitEpsilon = 1e-4f;   // src/rtcore/RayTriIntersection.cpp:6

@@ -203,7 +203,7 @@ extern "C" rtg_status rtg_grid_build_noalloc(const float* d_verts, int64_t nvert
         e = cudaMemcpyAsync(params, &hp, sizeof(GridParams), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(reinterpret_cast<unsigned char*>(work) + offsetof(BuildWork, nsort), 0,
-                                3 * sizeof(uint32_t), st);
+                                sizeof(BuildWork::nsort), st);
         if (e != cudaSuccess) return failure(RTG_DEVICE_ERROR, "upload resolved parameters", e);
         if (hp.status & (ST_CELL_CAP | ST_TOO_BIG)) break;
         a.skip_bbox = true;

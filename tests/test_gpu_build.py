@@ -46,10 +46,10 @@ def test_deforming_sphere(gridlib, oracle, k, frame):
     sc = scenes.deforming_sphere(frame)
     s, g = _check_grid(gridlib, oracle, sc.verts, sc.idx, k)
     if k == 2:
-        # the pole cells exercise the warp shared-slice sort (33..256) and
-        # the block bitonic sort (257..4096)
+        # every sort class but the bitmap one: thread (2..8), warp lanes
+        # (9..32), warp registers (33..256), block bitonic (257..4096)
         counts = np.diff(g.offsets)
-        for lo, hi in ((33, 256), (257, 4096)):
+        for lo, hi in ((2, 8), (9, 32), (33, 256), (257, 4096)):
             assert ((counts >= lo) & (counts <= hi)).any(), (lo, hi)
 
 
@@ -57,8 +57,9 @@ def test_skewed_density(gridlib, oracle):
     sc = scenes.skewed_density()
     s, g = _check_grid(gridlib, oracle, sc.verts, sc.idx, 4)
     counts = np.diff(g.offsets)
-    # per-cell sort classes: block bitonic (257..4096), block bitmap (>4096)
-    for lo, hi in ((2, 32), (257, 4096), (4097, 1 << 30)):
+    # per-cell sort classes: thread (2..8) and warp lanes (9..32) sharing
+    # one queue from both ends, block bitonic (257..4096), block bitmap (>4096)
+    for lo, hi in ((2, 8), (9, 32), (257, 4096), (4097, 1 << 30)):
         assert ((counts >= lo) & (counts <= hi)).any(), (lo, hi)
 
 
