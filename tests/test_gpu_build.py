@@ -63,6 +63,23 @@ def test_skewed_density(gridlib, oracle):
         assert ((counts >= lo) & (counts <= hi)).any(), (lo, hi)
 
 
+@pytest.mark.parametrize("n,k", [(1 << 18, 4), (1 << 20, 8), (1 << 22, 1)])
+def test_crowded_cells_rebuild(gridlib, oracle, n, k):
+    """Crowded cells, built and rebuilt in one scene: the same bits every time
+    and the oracle's.  1M triangles at k = 8 is the skewed benchmark's grid
+    (lists up to 70,153, all ids inside one bitmap span: the block sort reads
+    the list directly); 4M triangles at k = 1 has lists of ids spread over
+    more than one bitmap span (scratch copy, chunked bitmap passes)."""
+    sc = scenes.skewed_density(n=n)
+    s, g = _check_grid(gridlib, oracle, sc.verts, sc.idx, k)
+    assert np.diff(g.offsets).max() >= 1024
+    for _ in range(2):
+        s.build(k)
+        off, ids = s.download()
+        assert np.array_equal(off, g.offsets), "offsets differ"
+        assert np.array_equal(ids, g.ids), "sorted cell lists differ"
+
+
 def test_single_and_planar(gridlib, oracle):
     # one triangle in the z = 0 plane: planar box axis gets the 0.01 tolerance
     v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
