@@ -909,18 +909,32 @@ __device__ __forceinline__ void block_walk(const SParams& P, const SceneView& s,
             if (threadIdx.x == 0) tests += (uint32_t)(e - b);
             Lane T = L;
             T.id = -1;
+            // two entries a thread per step, both loaded before either is
+            // tested (the same entries in the same order as one a step)
             if (s.crec) {
-                for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
+                for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += 2 * kHugeThreads) {
+                    const int32_t i2 = i + kHugeThreads;
                     const float4 A = __ldg(s.crec + 3 * (int64_t)i), B = __ldg(s.crec + 3 * (int64_t)i + 1),
                                  C = __ldg(s.crec + 3 * (int64_t)i + 2);
+                    float4 A2 = A, B2 = B, C2 = C;
+                    if (i2 < e) {
+                        A2 = __ldg(s.crec + 3 * (int64_t)i2);
+                        B2 = __ldg(s.crec + 3 * (int64_t)i2 + 1);
+                        C2 = __ldg(s.crec + 3 * (int64_t)i2 + 2);
+                    }
                     test_tri<MODE_NEAREST>(T, __float_as_int(A.w), A, B, C, hi);
+                    if (i2 < e) test_tri<MODE_NEAREST>(T, __float_as_int(A2.w), A2, B2, C2, hi);
                 }
             } else {
-                for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
-                    const int32_t t = __ldg(s.ids + i);
+                for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += 2 * kHugeThreads) {
+                    const int32_t i2 = i + kHugeThreads;
+                    const int32_t t = __ldg(s.ids + i), t2 = i2 < e ? __ldg(s.ids + i2) : t;
                     const float4 A = __ldg(s.tris + 3 * (int64_t)t), B = __ldg(s.tris + 3 * (int64_t)t + 1),
                                  C = __ldg(s.tris + 3 * (int64_t)t + 2);
+                    const float4 A2 = __ldg(s.tris + 3 * (int64_t)t2), B2 = __ldg(s.tris + 3 * (int64_t)t2 + 1),
+                                 C2 = __ldg(s.tris + 3 * (int64_t)t2 + 2);
                     test_tri<MODE_NEAREST>(T, t, A, B, C, hi);
+                    if (i2 < e) test_tri<MODE_NEAREST>(T, t2, A2, B2, C2, hi);
                 }
             }
             // ids ascend along a list: the smaller id is the earlier entry
@@ -1462,6 +1476,20 @@ static void launch_wide(const SceneView& s, const TraceIO& io, const TraceTuning
     else launch_wide_g<MODE, COUNT, 32>(s, io, num_sms, st);
 }
 
+// As many blocks as fit on the GPU claim the queued rays: each ray's lists
+// are long latency chains, so the pass runs as many rays side by side as it
+// can hold.
+template <int MODE, bool COUNT>
+static void launch_huge(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_huge_kernel<MODE, COUNT>, kHugeThreads, 0);
+        per_sm = b > 0 ? b : 1;
+    }
+    launch_k(trace_huge_kernel<MODE, COUNT>, (unsigned)(per_sm * num_sms), kHugeThreads, 0, st, s, io);
+}
+
 template <int MODE>
 static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, const TraceTuning& tune, int num_sms,
                         cudaStream_t st) {
@@ -1482,9 +1510,8 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
         else launch_wide<MODE, false>(s, io, tune, num_sms, st);
     }
     if (io.huge) {
-        // two blocks per SM claim the queued rays
-        if (io.ctr) launch_k(trace_huge_kernel<MODE, true>, (unsigned)(2 * num_sms), kHugeThreads, 0, st, s, io);
-        else launch_k(trace_huge_kernel<MODE, false>, (unsigned)(2 * num_sms), kHugeThreads, 0, st, s, io);
+        if (io.ctr) launch_huge<MODE, true>(s, io, num_sms, st);
+        else launch_huge<MODE, false>(s, io, num_sms, st);
     }
 }
 
