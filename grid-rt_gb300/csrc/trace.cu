@@ -891,7 +891,11 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
 // the minimum t, ties to the earlier entry -- the one-lane walk's result, as
 // in the group pass.  A ray's walk then takes a block's time per list, not a
 // lane's or a group's.
-static constexpr int kHugeThreads = 256;
+#ifndef GRIDRT_HUGE_THREADS
+#define GRIDRT_HUGE_THREADS 256
+#endif
+static constexpr int kHugeThreads = GRIDRT_HUGE_THREADS;
+static_assert(kHugeThreads % 32 == 0 && kHugeThreads <= 1024, "block-per-ray pass: whole warps, one block");
 
 // The block's ray (identical state on every thread) walked to its end:
 // each list split over the block, a block reduction per list.

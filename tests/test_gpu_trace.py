@@ -227,8 +227,9 @@ def test_heavy_cell_counters_match_oracle(gridlib, oracle):
 def test_huge_list_block_pass_is_exact(gridlib, oracle):
     """Lists above 2,048 entries (59,000 triangles in a 0.1^3 cluster, k = 4)
     go from the group pass to the block-per-ray pass: hit words, frame
-    outputs, occlusion and traversal counters equal the one-lane walk's, and
-    the hits meet the oracle's near-tie rules."""
+    outputs, occlusion and traversal counters equal the one-lane walk's (with
+    the records read through the id lists and in cell order), and the hits
+    meet the oracle's near-tie rules."""
     sc = scenes.skewed_density(n=1 << 16)
     s = _scene(gridlib, sc, 4)      # a synchronous build: the scene knows its longest list
     g = oracle.Grid(sc.verts, sc.idx, 4)
@@ -244,8 +245,10 @@ def test_huge_list_block_pass_is_exact(gridlib, oracle):
     c0 = s.counters(reset=True)
     o0 = s.trace_any(rays_any)
     f0 = _frame(s, cam)
-    for lanes in (8, 32):
-        s.set_tuning(heavy_cell=32, heavy_lanes=lanes)
+    for lanes, records in ((8, False), (32, False), (32, True)):
+        s.set_tuning(heavy_cell=32, heavy_lanes=lanes, cell_records=records)
+        if records:
+            s.build(4)              # the records are written by the build
         h1 = s.trace_nearest(rays, counters=True)
         c1 = s.counters(reset=True)
         assert np.array_equal(h0.view(np.int32), h1.view(np.int32)), lanes
