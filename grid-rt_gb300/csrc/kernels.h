@@ -127,11 +127,12 @@ inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
     cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
-// Per-launch device state of a single-scene trace: three counters the launch
-// zeroes (ray claims, deferred rays, deferred claims) and the deferred-ray
-// queue; launches that may overlap need distinct slots.
+// Per-launch device state of a single-scene trace: the counters the launch
+// zeroes and the deferred-ray and huge-list queues; launches that may overlap
+// need distinct slots.
 struct TraceSlot {
-    unsigned long long* ctr;   // 8 words: ray claims, deferred rays, deferred claims, huge rays, huge claims
+    unsigned long long* ctr;   // 8 words: ray claims, deferred rays, deferred claims, huge rays, huge claims,
+                               // huge entries at the queue's back (lists of kHugeLong+), at its front
     int2* defer;          // {ray, cell} entries
     int32_t defer_cap;
     int2* huge = nullptr; // {ray, cell} entries of rays at a list above kHugeList (nullptr: no block pass)
@@ -140,6 +141,9 @@ struct TraceSlot {
 // Lists longer than this are tested by a whole block (the block-per-ray pass)
 // when the trace's slot has a huge-list queue.
 static constexpr int32_t kHugeList = 2048;
+// Huge-list queue entries at lists of at least this many entries are claimed
+// first by the block-per-ray pass.
+static constexpr int32_t kHugeLong = 8 * kHugeList;
 
 void launch_trace_nearest(const SceneView& s, const float4* rays, int64_t n, int4* hits, TraceCounters* ctr,
                           const TraceSlot& slot, const TraceTuning& tune, int num_sms, cudaStream_t st);

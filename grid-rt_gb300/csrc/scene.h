@@ -33,7 +33,7 @@ struct rtg_scene_s {
     int64_t cell_cap = 0;
     uint32_t* d_occ = nullptr;
     int64_t occ_cap = 0;
-    unsigned long long* d_ray_ctr = nullptr;   // ring of per-launch counters, 4 words a slot
+    unsigned long long* d_ray_ctr = nullptr;   // ring of per-launch counters, 8 words a slot
     int2* d_defer = nullptr;                   // ring of per-launch deferred-ray queues (tune.heavy_cell)
     unsigned ctr_seq = 0;
     gridrt::TraceTuning tune;

@@ -762,7 +762,14 @@ __device__ __forceinline__ bool wide_walk(const SParams& P, const SceneView& s, 
                 at = __shfl_sync(FULL, at, (int)(threadIdx.x & 31) & ~(G - 1));
                 if (want && at < (unsigned long long)huge_cap) {
                     if (gl == 0) {
-                        huge[at] = make_int2(huge_tag, L.x + L.y * nx + L.z * nxy);
+                        // longest first: lists of kHugeLong+ entries fill the
+                        // queue from its back (huge_ctr[2] of them), the rest
+                        // from its front (huge_ctr[3]); together they number
+                        // the reservations that fit, so the two never meet
+                        const bool longl = e - b >= kHugeLong;
+                        const unsigned long long pos = atomicAdd(huge_ctr + (longl ? 2 : 3), 1ull);
+                        huge[longl ? (unsigned long long)huge_cap - 1 - pos : pos] =
+                            make_int2(huge_tag, L.x + L.y * nx + L.z * nxy);
                         --cells;
                     }
                     handed = done = true;
@@ -990,6 +997,9 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
     load_sparams(s.params, P);
     unsigned long long nh = io.counter[3];
     if (nh > (unsigned long long)io.huge_cap) nh = (unsigned long long)io.huge_cap;
+    // the rays at the longest lists (the queue's back) are claimed first, so
+    // they do not start last and run on alone at the end of the pass
+    const unsigned long long nb = io.counter[5];
     uint32_t cells = 0, tests = 0;
     for (;;) {
         if (threadIdx.x == 0) claim = atomicAdd(io.counter + 4, 1ull);
@@ -997,7 +1007,7 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
         const unsigned long long j = claim;
         __syncthreads();
         if (j >= nh) break;
-        const int2 d = __ldg(io.huge + j);
+        const int2 d = __ldg(io.huge + (j < nb ? (unsigned long long)io.huge_cap - 1 - j : j - nb));
         const bool shadow = MODE == MODE_FRAME && d.x < 0;   // MODE_FRAME: a shadow ray (in its slot)
         Lane L;
         L.ray = shadow ? -1 - d.x : d.x;
@@ -1506,7 +1516,7 @@ static void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.huge = defer ? slot.huge : nullptr;
     io.huge_cap = io.huge ? slot.huge_cap : 0;
     count_launches(defer ? (io.huge ? 3 : 2) : 1);
-    cudaMemsetAsync(slot.ctr, 0, 5 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(slot.ctr, 0, 7 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {
