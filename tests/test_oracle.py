@@ -58,6 +58,24 @@ def test_restatement_equals_reference_plane(oracle):
         assert np.array_equal(_bits(hr[k]), _bits(ho[k])), k
 
 
+def test_restatement_equals_reference_crowded(oracle):
+    """A skewed-density scene (90% of the triangles in a 0.1^3 cluster): a
+    cell list of tens of thousands of entries, and rays into the cluster."""
+    _ref(oracle)
+    sc = scenes.skewed_density(n=1 << 15)
+    ref = oracle.RefScene(sc.verts, sc.idx)
+    g = oracle.Grid(sc.verts, sc.idx, oracle.RefScene.K)
+    off, ids = ref.csr()
+    assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
+    assert np.diff(off).max() > 4096      # one cluster cell of 29,491 entries at k = 6
+    rng = np.random.default_rng(7)
+    rays = np.concatenate([scenes.camera_rays(scenes.skewed_density_camera(96, 96)),
+                           scenes.random_rays(rng, 3000, (-0.06,) * 3, (0.06,) * 3)])
+    hr, ho = ref.trace(rays), g.trace_closest(rays)
+    for k in ("id", "t", "u", "v"):
+        assert np.array_equal(_bits(hr[k]), _bits(ho[k])), k
+
+
 def test_grid_walk_equals_brute_force_mostly(oracle):
     """Sanity of the reference itself: the grid walk returns the brute-force
     closest hit for almost every ray (exceptions are the reference's own
