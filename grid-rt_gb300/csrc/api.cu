@@ -116,6 +116,7 @@ BuildArgs make_args(rtg_scene s, int32_t k, bool skip_bbox) {
     a.params = s->d_params;
     a.work = s->d_work;
     a.tris = s->d_tris;
+    a.wald = s->d_wald;
     a.offsets = s->d_offsets;
     a.occ = s->d_occ;
     a.cell_cap = s->cell_cap < s->occ_cap ? s->cell_cap : s->occ_cap;
@@ -251,6 +252,7 @@ SceneView scene_view(rtg_scene s) {
     v.occ = s->d_occ;
     v.crec = (s->tune.cell_records && s->crec_built) ? s->d_crec : nullptr;
     v.tris = s->d_tris;
+    v.wald = s->d_wald;
     return v;
 }
 }  // namespace gridrt
@@ -343,6 +345,7 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
     cudaFree(s->d_verts);
     cudaFree(s->d_idx);
     cudaFree(s->d_tris);
+    cudaFree(s->d_wald);
     cudaFree(s->d_params);
     if (s->h_params) cudaFreeHost(s->h_params);
     cudaFree(s->d_work);
@@ -404,6 +407,7 @@ static rtg_status set_geometry(rtg_scene s, const float* verts, int64_t nverts, 
     CUDA_TRY(grow(s->d_verts, s->verts_cap, 3 * nverts + 4));
     CUDA_TRY(grow(s->d_idx, s->idx_cap, 3 * ntris + 4));
     CUDA_TRY(grow(s->d_tris, s->tris_cap, 3 * ntris + 3));
+    CUDA_TRY(grow(s->d_wald, s->wald_cap, 3 * ntris + 3));
     if (nverts) CUDA_TRY(cudaMemcpyAsync(s->d_verts, verts, sizeof(float) * 3 * nverts, kind, st));
     if (ntris) CUDA_TRY(cudaMemcpyAsync(s->d_idx, tris, sizeof(int32_t) * 3 * ntris, kind, st));
     s->nverts = nverts;

@@ -262,6 +262,42 @@ __device__ __forceinline__ void tri_box_range(const Lite& L, const float3& v0, c
     }
 }
 
+// TriAccel::buildFrom (src/rtcore/Triangle.cpp:11-55): Wald's projection
+// record, 48 bytes {k, n_u, n_v, n_d}, {b_nu, b_nv, b_d, 0}, {c_nu, c_nv,
+// c_d, id}, every operation rounded once in float as the reference's code
+// evaluates it (no contraction; IEEE division and reciprocal).  The trace
+// evaluates the winning triangle's t / u / v from it exactly as
+// RayTriIntersection::hitWald does, so a hit on the reference's triangle
+// reports the reference's bits.
+__device__ __forceinline__ float comp3(float x, float y, float z, uint32_t d) {
+    return d == 0 ? x : (d == 1 ? y : z);
+}
+__device__ __forceinline__ void write_wald_record(float4* __restrict__ out, const float3& v0, const float3& v1,
+                                                  const float3& v2, int32_t id) {
+    const float bx = fsub(v2.x, v0.x), by = fsub(v2.y, v0.y), bz = fsub(v2.z, v0.z);
+    const float cx = fsub(v1.x, v0.x), cy = fsub(v1.y, v0.y), cz = fsub(v1.z, v0.z);
+    // normal = c x b
+    const float nx = fsub(fmul(cy, bz), fmul(cz, by));
+    const float ny = fsub(fmul(cz, bx), fmul(cx, bz));
+    const float nz = fsub(fmul(cx, by), fmul(cy, bx));
+    uint32_t k;
+    if (vabs(nx) > vabs(ny) && vabs(nx) > vabs(nz)) k = 0;
+    else if (vabs(ny) > vabs(nz)) k = 1;
+    else k = 2;
+    const uint32_t u = k == 2 ? 0 : k + 1, v = k == 0 ? 2 : k - 1;
+    const float nk = comp3(nx, ny, nz, k), nu = comp3(nx, ny, nz, u), nv = comp3(nx, ny, nz, v);
+    const float inv_nk = frcp(nk);
+    const float nd = fadd(fadd(fmul(v0.x, fmul(nx, inv_nk)), fmul(v0.y, fmul(ny, inv_nk))), fmul(v0.z, fmul(nz, inv_nk)));
+    const float bu = comp3(bx, by, bz, u), bv = comp3(bx, by, bz, v);
+    const float cu = comp3(cx, cy, cz, u), cv = comp3(cx, cy, cz, v);
+    const float v0u = comp3(v0.x, v0.y, v0.z, u), v0v = comp3(v0.x, v0.y, v0.z, v);
+    const float inv_den = frcp(fsub(fmul(bu, cv), fmul(bv, cu)));
+    out[0] = make_float4(__uint_as_float(k), fdiv(nu, nk), fdiv(nv, nk), nd);
+    out[1] = make_float4(fmul(-bv, inv_den), fmul(bu, inv_den), fmul(fsub(fmul(bv, v0u), fmul(bu, v0v)), inv_den), 0.0f);
+    out[2] = make_float4(fmul(cv, inv_den), fmul(-cu, inv_den), fmul(fsub(fmul(cu, v0v), fmul(cv, v0u)), inv_den),
+                         __int_as_float(id));
+}
+
 __device__ __forceinline__ float3 load_vert(const float* __restrict__ verts, int32_t v) {
     const float* q = verts + 3 * (int64_t)v;
     return make_float3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
@@ -272,8 +308,8 @@ __device__ __forceinline__ float3 load_vert(const float* __restrict__ verts, int
 template <bool WRITE_TRIS, class Emit>
 __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restrict__ verts,
                                             const int32_t* __restrict__ idx, int64_t ntris, int64_t base,
-                                            float4* __restrict__ tris, GridParams* p, BuildWork* w,
-                                            Emit&& emit) {
+                                            float4* __restrict__ tris, float4* __restrict__ wald, GridParams* p,
+                                            BuildWork* w, Emit&& emit) {
     const int lane = threadIdx.x & 31;
     const int64_t t = base + lane;
     int32_t lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
@@ -299,6 +335,7 @@ __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restri
             tris[3 * t + 0] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int32_t)t));
             tris[3 * t + 1] = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.0f);
             tris[3 * t + 2] = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.0f);
+            if (wald) write_wald_record(wald + 3 * t, v0, v1, v2, (int32_t)t);
         }
     }
     unsigned long long incl = cnt;
@@ -338,7 +375,8 @@ __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restri
 
 __device__ __forceinline__ void count_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
                                                     int64_t ntris, GridParams* p, BuildWork* w,
-                                                    int32_t* __restrict__ counts, float4* __restrict__ tris, unsigned vbx, unsigned vgx) {
+                                                    int32_t* __restrict__ counts, float4* __restrict__ tris,
+                                                    float4* __restrict__ wald, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     Lite L;
     load_lite(p, L);
@@ -346,7 +384,7 @@ __device__ __forceinline__ void count_body(const float* __restrict__ verts, cons
     const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
-        warp_expand<true>(L, verts, idx, ntris, base, tris, p, w, [&](int32_t cell, int32_t, bool active) {
+        warp_expand<true>(L, verts, idx, ntris, base, tris, wald, p, w, [&](int32_t cell, int32_t, bool active) {
             const unsigned peers = __match_any_sync(FULL, cell);
             const int leader = __ffs(peers) - 1;
             if (active && lane == leader) atomicAdd(&counts[cell], __popc(peers));
@@ -361,10 +399,11 @@ __global__ void __launch_bounds__(256) count_kernel(BuildArgs one, const BuildAr
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
-        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
+        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, a.wald, blockIdx.x - (unsigned)first[t],
+                   (unsigned)(first[t + 1] - first[t]));
     } else {
         const BuildArgs& a = one;
-        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, blockIdx.x, gridDim.x);
+        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, a.wald, blockIdx.x, gridDim.x);
     }
 }
 

@@ -19,6 +19,7 @@ struct BuildArgs {
     GridParams* params;
     BuildWork* work;
     float4* tris;          // 3 per triangle
+    float4* wald;          // 3 per triangle: TriAccel records (nullptr: not written)
     int32_t* offsets;      // cell_cap entries
     uint32_t* occ;         // occupancy bitmap, cell_cap words (nullptr: not built)
     int64_t cell_cap;
@@ -78,6 +79,7 @@ struct SceneView {
     const uint32_t* occ;
     const float4* crec;    // records in cell-list order, or nullptr (then ids -> tris)
     const float4* tris;
+    const float4* wald;    // TriAccel records: the reported t / u / v of a hit (nullptr: from tris)
 };
 
 struct CameraArgs {

@@ -172,6 +172,7 @@ extern "C" rtg_status rtg_grid_build_noalloc(const float* d_verts, int64_t nvert
     a.params = params;
     a.work = work;
     a.tris = reinterpret_cast<float4*>(d_tri_records);
+    a.wald = nullptr;  // hit-value records serve only the scene's trace kernels
     a.offsets = d_offsets;
     a.occ = nullptr;   // the occupancy bitmap only serves the scene's trace kernels
     a.crec = nullptr;

@@ -25,6 +25,8 @@ struct rtg_scene_s {
     int64_t idx_cap = 0, ntris = 0;      // capacity in ints
     float4* d_tris = nullptr;
     int64_t tris_cap = 0;                // float4 records
+    float4* d_wald = nullptr;            // TriAccel records, 3 float4 a triangle
+    int64_t wald_cap = 0;
 
     gridrt::GridParams* d_params = nullptr;
     gridrt::GridParams* h_params = nullptr;      // pinned mirror

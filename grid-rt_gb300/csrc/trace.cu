@@ -309,41 +309,39 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
     return false;
 }
 
-// Reported hit values of the winning triangle.  Moller-Trumbore's u, v and t
-// come from dot products of the (large) origin-to-vertex vector, which cancel
-// badly for small triangles seen from far away; the winner's t is therefore
-// re-derived from the plane equation t = ((v0 - o).n) / (d.n) and u, v from
-// the hit point P = o + t*d projected on the triangle's dominant plane (the
-// quantities Wald's test evaluates, src/rtcore/RayTriIntersection.cpp:15-47).
-// The accept / reject decisions stay Moller-Trumbore's.
-__device__ __forceinline__ int4 refined_hit(const float4* __restrict__ tris, const Lane& L) {
-    const float4 A = __ldg(tris + 3 * (int64_t)L.id);
-    const float4 B = __ldg(tris + 3 * (int64_t)L.id + 1);
-    const float4 C = __ldg(tris + 3 * (int64_t)L.id + 2);
-    const float nx = B.y * C.z - B.z * C.y, ny = B.z * C.x - B.x * C.z, nz = B.x * C.y - B.y * C.x;
-    const float num = (A.x - L.ox) * nx + (A.y - L.oy) * ny + (A.z - L.oz) * nz;
-    const float den = L.dx * nx + L.dy * ny + L.dz * nz;
-    const float t = num / den;
-    const float wx = (L.ox + t * L.dx) - A.x, wy = (L.oy + t * L.dy) - A.y, wz = (L.oz + t * L.dz) - A.z;
-    const float ax = fabsf(nx), ay = fabsf(ny), az = fabsf(nz);
-    float e1a, e1b, e2a, e2b, wa, wb;
-    if (ax > ay && ax > az) {
-        e1a = B.y; e1b = B.z; e2a = C.y; e2b = C.z; wa = wy; wb = wz;
-    } else if (ay > az) {
-        e1a = B.z; e1b = B.x; e2a = C.z; e2b = C.x; wa = wz; wb = wx;
-    } else {
-        e1a = B.x; e1b = B.y; e2a = C.x; e2b = C.y; wa = wx; wb = wy;
+// Reported hit values of the winning triangle: RayTriIntersection::hitWald
+// (src/rtcore/RayTriIntersection.cpp:12-48) on the triangle's TriAccel record
+// (written by the build exactly as TriAccel::buildFrom computes it), with the
+// reference's operation order and one rounding per operation.  The accept /
+// reject decisions of the walk stay Moller-Trumbore's; when the walk's winner
+// is the reference's triangle, t (hitWald's f), u (lambda) and v (mue) are the
+// reference's bits.
+__device__ __forceinline__ float pick3(float x, float y, float z, uint32_t d) {
+    return d == 0 ? x : (d == 1 ? y : z);
+}
+__device__ __forceinline__ int4 wald_hit(const float4* __restrict__ wald, const Lane& L) {
+    const float4 a0 = __ldg(wald + 3 * (int64_t)L.id);
+    const float4 a1 = __ldg(wald + 3 * (int64_t)L.id + 1);
+    const float4 a2 = __ldg(wald + 3 * (int64_t)L.id + 2);
+    const uint32_t k = __float_as_uint(a0.x);
+    const uint32_t ku = k == 2 ? 0 : k + 1, kv = k == 0 ? 2 : k - 1;
+    const float dk = pick3(L.dx, L.dy, L.dz, k), du = pick3(L.dx, L.dy, L.dz, ku), dv = pick3(L.dx, L.dy, L.dz, kv);
+    const float ok = pick3(L.ox, L.oy, L.oz, k), ou = pick3(L.ox, L.oy, L.oz, ku), ov = pick3(L.ox, L.oy, L.oz, kv);
+    const float nd = frcp(fadd(fadd(dk, fmul(a0.y, du)), fmul(a0.z, dv)));
+    const float f = fmul(nd, fsub(fsub(fsub(a0.w, ok), fmul(a0.y, ou)), fmul(a0.z, ov)));
+    const float hu = fadd(ou, fmul(f, du));
+    const float hv = fadd(ov, fmul(f, dv));
+    float lambda = fadd(fadd(fmul(hu, a1.x), fmul(hv, a1.y)), a1.z);
+    float mue = fadd(fadd(fmul(hu, a2.x), fmul(hv, a2.y)), a2.z);
+    float t = f;
+    if (!(isfinite(f) && isfinite(lambda) && isfinite(mue))) {
+        // a triangle without a finite projection record (the reference drops
+        // such triangles at ingest): keep the walk's t
+        t = L.best;
+        lambda = 0.0f;
+        mue = 0.0f;
     }
-    const float D = e1a * e2b - e2a * e1b;
-    float u = (wa * e2b - e2a * wb) / D;
-    float v = (e1a * wb - wa * e1b) / D;
-    float tt = t;
-    if (!(isfinite(t) && isfinite(u) && isfinite(v))) {
-        tt = L.best;   // degenerate refinement: keep the decision's t
-        u = 0.0f;
-        v = 0.0f;
-    }
-    return make_int4(L.id, __float_as_int(tt), __float_as_int(u), __float_as_int(v));
+    return make_int4(L.id, __float_as_int(t), __float_as_int(lambda), __float_as_int(mue));
 }
 
 __device__ __forceinline__ void ray_pixel(int32_t i, const CameraArgs& cam, int32_t& px, int32_t& py) {
@@ -449,15 +447,17 @@ __device__ __forceinline__ float3 cosine_dir(float nx, float ny, float nz, unsig
 // on with a follow-up ray: MODE_FRAME's camera phase sets up the hit's shadow
 // ray in the lane, from the same values it writes to the shadow-ray slot.
 template <int MODE>
-__device__ __forceinline__ bool finish_ray(const TraceIO& io, const SParams& P, const float4* __restrict__ tris,
-                                           Lane& L, bool write = true) {
+__device__ __forceinline__ bool finish_ray(const TraceIO& io, const SParams& P, const SceneView& sv, Lane& L,
+                                           bool write = true) {
+    const float4* __restrict__ tris = sv.tris;
+    const float4* __restrict__ wald = sv.wald;
     const int64_t r = L.ray;
     if (MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax)) {
         if (write) io.occ[r] = L.id == -2 ? 2 : (L.id >= 0 ? 1 : 0);
         return false;
     }
     int4 h = make_int4(-1, 0, 0, 0);
-    if (L.id >= 0) h = refined_hit(tris, L);
+    if (L.id >= 0) h = wald_hit(wald, L);
     if (write) io.hits[r] = h;
     if (MODE == MODE_CAMERA || MODE == MODE_FRAME) {
         float4 sa = make_float4(0.f, 0.f, 0.f, kRayEpsilon), sb = make_float4(0.f, 0.f, 0.f, -1.0f);
@@ -540,7 +540,7 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
         ++started;
         if (!start_ray<MODE>(P, io, L, L.ray)) {
             if (L.id != -2) L.id = -1;
-            active = finish_ray<MODE>(io, P, s.tris, L);
+            active = finish_ray<MODE>(io, P, s, L);
         }
     }
     while (__any_sync(FULL, active)) {
@@ -570,7 +570,7 @@ __device__ __forceinline__ void trace_batch32(const SParams& P, const SceneView&
                 }
             }
         }
-        if (fin) active = finish_ray<MODE>(io, P, s.tris, L);
+        if (fin) active = finish_ray<MODE>(io, P, s, L);
     }
 }
 
@@ -626,7 +626,7 @@ __device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& 
                         active = true;
                     } else {
                         if (L.id != -2) L.id = -1;
-                        active = finish_ray<MODE>(io, P, s.tris, L);
+                        active = finish_ray<MODE>(io, P, s, L);
                     }
                 }
             }
@@ -660,7 +660,7 @@ __device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& 
                 }
             }
         }
-        if (fin) active = finish_ray<MODE>(io, P, s.tris, L);
+        if (fin) active = finish_ray<MODE>(io, P, s, L);
     }
 }
 
@@ -875,13 +875,13 @@ __global__ void __launch_bounds__(128) trace_wide_kernel(SceneView s, TraceIO io
             // a camera ray's group goes on with its hit's shadow ray: every
             // lane sets it up from the hit (one writes the results)
             bool second = false;
-            if (valid && !handed) second = finish_ray<MODE>(io, P, s.tris, L, gl == 0);
+            if (valid && !handed) second = finish_ray<MODE>(io, P, s, L, gl == 0);
             bool done2 = !second;
             const bool handed2 = wide_walk<G>(P, s, L, done2, true, cells, tests, io.huge, io.huge_cap,
                                               io.counter + 3, -1 - L.ray);
-            if (second && !handed2 && gl == 0) finish_ray<MODE>(io, P, s.tris, L);
+            if (second && !handed2 && gl == 0) finish_ray<MODE>(io, P, s, L);
         } else if (valid && gl == 0 && !handed) {
-            finish_ray<MODE>(io, P, s.tris, L);
+            finish_ray<MODE>(io, P, s, L);
         }
     }
     if (COUNT) {
@@ -1023,7 +1023,7 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
         for (int phase = 0; phase < 2; ++phase) {
             block_walk(P, s, L, done, MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax), cells, tests,
                        red_t, red_id);
-            if (!finish_ray<MODE>(io, P, s.tris, L, threadIdx.x == 0)) break;
+            if (!finish_ray<MODE>(io, P, s, L, threadIdx.x == 0)) break;
             done = false;
         }
     }
@@ -1090,7 +1090,7 @@ __device__ __forceinline__ unsigned long long trace_task_refill(const SParams& P
                         active = true;
                     } else {
                         if (L.id != -2) L.id = -1;
-                        finish_ray<MODE>(io, P, s.tris, L);
+                        finish_ray<MODE>(io, P, s, L);
                     }
                 }
             }
@@ -1126,7 +1126,7 @@ __device__ __forceinline__ unsigned long long trace_task_refill(const SParams& P
             }
         }
         if (fin) {
-            finish_ray<MODE>(io, P, s.tris, L);
+            finish_ray<MODE>(io, P, s, L);
             active = false;
         }
     }
@@ -1238,8 +1238,8 @@ __global__ void __launch_bounds__(128) trace_wide_batch_kernel(const BatchScene*
         const SceneView V = scenes[scene].view;
         wide_walk<G>(P[scene], V, L, done, any, cells, tests);
         if (valid && gl == 0) {
-            if (any) finish_ray<MODE_ANY>(io, P[scene], V.tris, L);
-            else finish_ray<MODE_NEAREST>(io, P[scene], V.tris, L);
+            if (any) finish_ray<MODE_ANY>(io, P[scene], V, L);
+            else finish_ray<MODE_NEAREST>(io, P[scene], V, L);
         }
     }
 }
@@ -1372,7 +1372,7 @@ __global__ void __launch_bounds__(128) trace_instances_kernel(const InstanceRec*
                     xf_dir(m, wd[0], wd[1], wd[2], L.dx, L.dy, L.dz);
                     L.id = gid;
                     L.best = gbest;
-                    h = refined_hit(R->view.tris, L);
+                    h = wald_hit(R->view.wald, L);
                 }
                 io.hits[r] = h;
                 if (inst_out) inst_out[r] = ginst;

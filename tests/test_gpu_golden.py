@@ -2,8 +2,9 @@
 CPU code (compiled unmodified) on small seeded scenes at the reference's
 k = 6, committed under tests/golden/ with the script that made them.  Grid
 parameters and cell lists bit for bit; closest hits under the near-tie rules
-of parity.py (the device intersects with Moller-Trumbore, the reference with
-Wald's projection test); shadow-ray occlusion up to near-ties."""
+of parity.py (the device decides hits with Moller-Trumbore, the reference with
+Wald's projection test; the reported t / u / v are Wald's); shadow-ray
+occlusion up to near-ties, each explained by its occluding triangle."""
 import glob
 import os
 
@@ -48,8 +49,9 @@ def test_device_matches_reference_golden(gridlib, oracle, path):
     if "shadow_rays" in z.files:
         sr = z["shadow_rays"]
         occ = s.trace_any(sr)
-        # a few hundred shadow rays from the surface: two near-ties at most
-        # (the two intersection tests round differently at edges and at the
-        # window bounds, as for the closest hits)
-        mism = int((occ != z["occluded"]).sum())
-        assert mism <= max(2, int(2e-3 * sr.shape[0])), mism
+        # every disagreement with the reference's occlusion is explained by
+        # the occluding triangle (an edge, or t at the window bounds); the
+        # oracle's closest hit stands in for the reference's on those rays
+        g = oracle.Grid(verts, idx, k)
+        parity.check_occlusion(os.path.basename(path), s, g, gridlib.split_hits, sr, occ, z["occluded"], verts,
+                               idx, oracle, max_tie_frac=2e-3)

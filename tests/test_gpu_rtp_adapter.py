@@ -50,4 +50,8 @@ def test_cpp_plugin_mirror(gridlib, oracle, tmp_path):
     oh = g.trace_closest(rays)
     st = parity.compare_hits(gh, oh, sc.verts, sc.idx, rays, oracle)
     parity.assert_parity(st)
-    assert np.array_equal(any_b, g.trace_any(anyr)) or (any_b != g.trace_any(anyr)).sum() <= 2
+    s = gridlib.Scene(0)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(4)
+    parity.check_occlusion("adapter", s, g, gridlib.split_hits, anyr, any_b, g.trace_any(anyr), sc.verts, sc.idx,
+                           oracle)
