@@ -1,23 +1,37 @@
-"""Benchmark: deforming-mesh per-frame rebuild + trace on one GB300.
+"""Benchmark: uniform-grid rebuild + 3D-DDA trace on one GB300.
 
-Workload (one "step" = one frame): a 160 x 320 x 2 = 102,400-triangle UV
-sphere (pole caps open) whose 51,520 vertices are displaced on the device by
-0.05*sin(3*p.x + 0.3*frame) along their normals; full uniform-grid rebuild
-(cells per triangle k in {2, 4, 8}); 1024 x 1024 primary camera rays; one
-shadow ray per lit-facing hit toward a point light, traced as any-hit.
-Frames cycle through 20 phases.
+Default run (one JSON line, rank 0):
 
-Prints ONE JSON line (rank 0).  `value` = (primary + shadow rays) / frame
-time, device-timed with CUDA events on the scene's stream, inputs resident,
-L2 flushed between frames, each frame (deform + build + trace) replayed from
-a CUDA graph captured per deformation phase; `per_k[k].stream_value` is the
-same frames launched one call at a time.  `e2e` = the same through the public C ABI with
-host buffers: host-deformed vertices uploaded from pinned memory, synchronous
-build, frame trace, hits + occlusion copied back every frame.
+* headline -- deforming-mesh per-frame rebuild.  One "step" = one frame: a
+  160 x 320 x 2 = 102,400-triangle UV sphere (pole caps open) whose 51,520
+  vertices are displaced on the device by 0.05*sin(3*p.x + 0.3*frame) along
+  their normals; full uniform-grid rebuild at k = 4 cells per triangle (k = 2
+  and 8 in `per_k`); 1024 x 1024 primary camera rays and one shadow ray per
+  lit-facing hit, traced as any-hit.  Frames cycle through 20 phases.
+  `value` = (primary + shadow rays) / frame time, device-timed with CUDA
+  events on the scene's stream, inputs resident, L2 flushed between frames,
+  each frame (deform + build + trace) replayed from a CUDA graph captured per
+  deformation phase.  `e2e` = the same frames through the public C ABI with
+  host buffers (keyframes from pinned host memory, hits and occlusion copied
+  back every frame), host-clocked.  `cpu_baseline` = the oracle restatement
+  of the reference's CPU path on the host cores (single-thread build, every
+  ray in 16 x 16 tiles).
+* `cfg0_plain` -- 65,536-triangle plane + debris scene, 512 x 512 rays and
+  their shadow rays, build + trace per step, with the CPU path timed beside it.
+* `cfg2_skewed` -- 1,048,576 triangles of skewed density, 1024 x 1024 primary
+  rays + one diffuse secondary ray per hit, build included; FP64 errors.
+* `cfg3_batched` -- 64 uneven scenes built and traced in one graph-captured
+  batch vs 64 sequential per-scene calls.
+* `cfg4_serving` -- 16 resident scenes, requests served by continuous
+  batching vs one at a time: saturation throughput and p50/p99 latency, and
+  latency at 1,000 requests/s.
+
+`--workload X` runs one workload alone and prints its full result;
+`--detail PATH` writes every workload's full result to PATH.
 
 --impl reference times the reference's CPU path (the oracle restatement of
 UniformGridAccStructBuilder + UniformGridAccStruct, compiled here) on the
-host cores on a bounded sample of the same workload.
+host cores, every ray of the headline workload.
 """
 from __future__ import annotations
 
@@ -39,6 +53,7 @@ from gridrt import scenes  # noqa: E402
 
 FRAMES = 20
 LAMBDAS = (2, 4, 8)
+HEADLINE_K = 4          # cells per triangle of the headline line (and of the CPU arms)
 WIDTH = HEIGHT = 1024
 METRIC = "Mrays/s (primary + shadow, per-frame rebuild included)"
 WORKLOAD = "deforming_sphere_102400tri_1024x1024_shadow"
@@ -180,8 +195,9 @@ def _sum_over_ranks(x: float, dist) -> float:
 # ---------------------------------------------------------------------------
 def cpu_frame_sample(k: int, frame: int, sample_stride: int, nthreads: int = 0):
     """Build the frame's grid single-threaded (the reference's build is), trace
-    every `sample_stride`-th primary ray plus the shadow rays of those hits on
-    all host threads; extrapolate to the full frame."""
+    every `sample_stride`-th primary ray (in 16 x 16 pixel tiles) plus the
+    shadow rays of those hits on all host threads; extrapolate to the full
+    frame."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
     sc = scenes.deforming_sphere(frame)
@@ -189,7 +205,9 @@ def cpu_frame_sample(k: int, frame: int, sample_stride: int, nthreads: int = 0):
     g = pyoracle.Grid(sc.verts, sc.idx, k)
     t_build = time.perf_counter() - t0
     cam = scenes.deforming_sphere_camera(WIDTH, HEIGHT)
-    rays = scenes.camera_rays(cam)[::sample_stride]
+    # 16 x 16 pixel tiles, one per OpenMP chunk (TiledRenderer's schedule,
+    # src/rtplugins/TiledRenderer.cpp:19-27)
+    rays = scenes.camera_rays(cam)[_tile_order(WIDTH, HEIGHT)][::sample_stride]
     t0 = time.perf_counter()
     h = g.trace_closest(rays, nthreads=nthreads)
     t_prim = time.perf_counter() - t0
@@ -228,12 +246,12 @@ def _host_shadow_rays(sc, rays, h, light):
 
 def run_reference(args, rank, ws, dist):
     if rank != 0:
-        return
+        return None
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
     pyoracle.build()
-    k = 4
-    stride = 4
+    k = HEADLINE_K
+    stride = 1
     for w in range(args.warmup):
         cpu_frame_sample(k, w % FRAMES, stride)
     res = [cpu_frame_sample(k, s % FRAMES, stride) for s in range(args.steps)]
@@ -241,9 +259,9 @@ def run_reference(args, rank, ws, dist):
     rays = sum(r["rays"] for r in res)
     value = rays / t / 1e6
     cores = res[0]["threads"]
-    sample = (f"per frame: full single-thread grid build (k={k}) + every {stride}th primary ray and its shadow "
-              f"ray traced on {cores} threads, trace time x{stride}")
-    print(json.dumps({
+    sample = (f"per frame: single-thread grid build (k={k}) + every 1024^2 primary ray and its shadow ray "
+              f"traced on {cores} threads")
+    return ({
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -251,7 +269,7 @@ def run_reference(args, rank, ws, dist):
         "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
                          "sample": sample, "build_ms": round(1e3 * statistics.median(r["t_build"] for r in res), 3)},
         "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }), flush=True)
+    })
 
 
 # ---------------------------------------------------------------------------
@@ -320,10 +338,12 @@ def run_gpu(args, rank, ws, local, dist):
     sampler = ClockSampler(local).start() if rank == 0 else None
     for k in ([fixed["k"]] if fixed else LAMBDAS):
         if fixed:
-            best, allres = {x: fixed[x] for x in fixed if x != "k"}, []
+            best, allres, source = {x: fixed[x] for x in fixed if x != "k"}, [], "fixed"
         else:
             best, allres = tune_k(k)
-        tuned[k] = dict(best=best, all=[(c, round(m, 4)) for c, m in allres])
+            source = "search"
+        tuned[k] = dict(best=best, all=[(c, round(m, 4)) for c, m in allres], source=source)
+        _save_autotune(f"deforming_k{k}", allres)
         order = best["order"]
         _apply_tuning(s, best)
         for w in range(args.warmup):
@@ -402,7 +422,7 @@ def run_gpu(args, rank, ws, local, dist):
     if sampler:
         sampler.stop()
 
-    best_k = max(per_k, key=lambda kk: per_k[kk]["value"])
+    best_k = HEADLINE_K if HEADLINE_K in per_k else max(per_k, key=lambda kk: per_k[kk]["value"])
     head = per_k[best_k]
     order = head["tuning"]["order"]
     _apply_tuning(s, head["tuning"])
@@ -437,7 +457,7 @@ def run_gpu(args, rank, ws, local, dist):
     kern_s = ev0.elapsed_time(ev1) / 1e3 / reps
     peak, peak_kind = _peaks()
     achieved = alg_bytes / kern_s / 1e9
-    traffic = _traffic_from_profiles("trace_frame", alg_bytes)
+    traffic = _traffic_from_profiles("trace_frame", best_k)
     l2_peak = _l2_read_gbs(dev)
     # build roofline: 12 N index bytes + 12 V vertex bytes + 4 (C + 1) offsets
     # + 4 R ids per build, over the median device-timed build
@@ -449,7 +469,7 @@ def run_gpu(args, rank, ws, local, dist):
     e2e = run_e2e(args, s, v, idx, nrm, cam, light, best_k, order, dist)
 
     if rank != 0:
-        return
+        return None
     cpu_frames = [cpu_frame_sample(best_k, f, 1) for f in range(0, FRAMES, 2)]   # 10 frames, every ray
     cpu = dict(t_build=statistics.median(c["t_build"] for c in cpu_frames),
                t_frame=sum(c["t_frame"] for c in cpu_frames), rays=sum(c["rays"] for c in cpu_frames),
@@ -466,7 +486,9 @@ def run_gpu(args, rank, ws, local, dist):
         "build_ms": round(head["build_ms"], 4), "trace_mrays_s": round(head["trace_mrays_s"], 2),
         "per_k": {str(kk): {x: (round(y, 4) if isinstance(y, float) else y) for x, y in d.items() if x != "tuning"}
                   for kk, d in per_k.items()},
-        "autotune": {str(kk): v["all"] for kk, v in tuned.items()},
+        "autotune": {str(kk): {"candidates": len(v["all"]), "source": v["source"],
+                               "best_ms": min((m for _, m in v["all"]), default=None),
+                               "worst_ms": max((m for _, m in v["all"]), default=None)} for kk, v in tuned.items()},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                      "kernel": "frame trace_kernel (camera rays, then each hit's shadow ray in the same lane) "
@@ -492,7 +514,7 @@ def run_gpu(args, rank, ws, local, dist):
         "clocks": {"sm_mhz": clocks.get("sm_mhz"), "sm_max_mhz": clocks.get("sm_max_mhz"),
                    "reasons": clocks.get("reasons", []), "samples": clocks.get("samples", 0)},
     }
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def _l2_read_gbs(dev) -> float:
@@ -514,16 +536,34 @@ def _cpu_model() -> str:
     return platform.processor() or platform.machine()
 
 
-def _traffic_from_profiles(kernel: str, alg_bytes: int):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/traffic.json), or None."""
+def _traffic_from_profiles(kernel: str, k: int):
+    """DRAM bytes per launch of `kernel` at cells-per-triangle k, from the
+    committed ncu summary (profiles/traffic.json), or None when that k was
+    not captured."""
     path = os.path.join(REPO, "profiles", "traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return d.get(kernel, {}).get("dram_bytes_per_launch")
+        e = d.get(kernel, {})
+        if int(e.get("k", -1)) != int(k):
+            return None
+        return e.get("dram_bytes_per_launch")
     except Exception:
         return None
+
+
+def _save_autotune(name: str, results):
+    """The full candidate table of one search, written beside the run's
+    output (directory from GRIDRT_BENCH_OUT, default gpurun_out/ when it
+    exists) instead of into the result line."""
+    out_dir = os.environ.get("GRIDRT_BENCH_OUT") or os.path.join(REPO, "gpurun_out")
+    if not results or not os.path.isdir(out_dir):
+        return
+    try:
+        with open(os.path.join(out_dir, f"autotune_{name}.json"), "w") as f:
+            json.dump([{"cfg": c, "ms": round(m, 4)} for c, m in results], f)
+    except OSError:
+        pass
 
 
 def run_e2e(args, s, v, idx, nrm, cam, light, k, order, dist):
@@ -579,6 +619,115 @@ def run_e2e(args, s, v, idx, nrm, cam, light, k, order, dist):
                    "(next keyframe from pinned host memory on a copy stream) + rtg_trace_frame_async (hits and "
                    "occlusion copied to pinned host memory on the scene's copy stream), and rtg_trace_frame_wait "
                    "for the previous frame's results; the clock stops after the last frame's results are on the host"}
+
+
+# ---------------------------------------------------------------------------
+# plain small scene, the case the reference's CPU path runs: 65,536 triangles
+# (a 128 x 128-quad ground plane and 32,768 small random triangles), k = 4,
+# 512 x 512 primary rays and one shadow ray per lit-facing hit; a step is one
+# grid build and the frame trace.  The CPU side is the oracle restatement of
+# the reference's path: a single-thread build, then the camera rays in 16 x 16
+# pixel tiles, one tile per OpenMP chunk (TiledRenderer's schedule), and the
+# shadow rays of their hits.
+# ---------------------------------------------------------------------------
+def _tile_order(width: int, height: int, tile: int = 16) -> np.ndarray:
+    """Scanline ray indices regrouped into tile x tile pixel tiles, row of
+    tiles after row of tiles."""
+    i = np.arange(width * height).reshape(height // tile, tile, width // tile, tile)
+    return i.transpose(0, 2, 1, 3).reshape(-1)
+
+
+def run_plain_small(args, rank, ws, local, dist):
+    import torch
+    from gridrt import lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc = scenes.plane_and_debris()
+    cam = scenes.plane_and_debris_camera(512, 512)
+    light = scenes.PLANE_LIGHT
+    npix = cam.width * cam.height
+    k = 4
+    s = lib.Scene(local)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(k)
+    stream = torch.cuda.ExternalStream(s.stream, device=dev)
+    d_hits = torch.empty((npix, 4), dtype=torch.int32, device=dev)
+    d_occ = torch.empty(npix, dtype=torch.uint8, device=dev)
+    d_sr = torch.empty((npix, 8), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    order = "morton8"
+
+    def step(ev=None):
+        with torch.cuda.stream(stream):
+            if ev:
+                ev[0].record(stream)
+            s.build_async(k)
+            if ev:
+                ev[1].record(stream)
+            s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order)
+            if ev:
+                ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for st in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        step(evs[st])
+    torch.cuda.synchronize()
+    build_ms = statistics.median(e[0].elapsed_time(e[1]) for e in evs)
+    trace_ms = statistics.median(e[1].elapsed_time(e[2]) for e in evs)
+    # the same step replayed from a CUDA graph (the headline's form)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        step()
+    g.replay()
+    torch.cuda.synchronize()
+    gevs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+    for st in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            gevs[st][0].record(stream)
+            g.replay()
+            gevs[st][1].record(stream)
+    torch.cuda.synchronize()
+    if s.build_check() != 0:
+        raise RuntimeError("plain-scene build failed: " + lib.load().rtg_last_error().decode())
+    g_ms = sum(e[0].elapsed_time(e[1]) for e in gevs) / args.steps
+    nshadow = int((d_occ != 2).sum().item())
+    rays = npix + nshadow
+    del g
+    if rank != 0:
+        return None
+    # CPU: the oracle restatement of the reference's build and trace
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    tiles = scenes.camera_rays(cam)[_tile_order(cam.width, cam.height)]
+    cpu = []
+    for rep in range(4):
+        t0 = time.perf_counter()
+        grid = pyoracle.Grid(sc.verts, sc.idx, k)
+        t1 = time.perf_counter()
+        h = grid.trace_closest(tiles)
+        t2 = time.perf_counter()
+        sr = _host_shadow_rays(sc, tiles, h, light)
+        t3 = time.perf_counter()
+        grid.trace_any(sr)
+        t4 = time.perf_counter()
+        if rep:                                   # the first repetition warms the caches
+            cpu.append((t1 - t0, (t2 - t1) + (t4 - t3), npix + sr.shape[0]))
+    cpu_s = sum(b + t for b, t, _ in cpu) / len(cpu)
+    cpu_rays = cpu[0][2]
+    return {"workload": "plane_debris_65536tri_512x512_shadow", "k": k, "value": round(rays / g_ms / 1e3, 2),
+            "ms_per_step": round(g_ms, 4), "build_ms": round(build_ms, 4),
+            "trace_ms": round(trace_ms, 4), "rays_per_step": rays, "steps": args.steps,
+            "cpu": {"value": round(cpu_rays / cpu_s / 1e6, 3), "ms_per_step": round(1e3 * cpu_s, 3),
+                    "build_ms": round(1e3 * statistics.median(b for b, _, _ in cpu), 3),
+                    "cores": pyoracle.max_threads(), "kind": "port", "steps": len(cpu)},
+            "vs_cpu": round((rays / g_ms / 1e3) / (cpu_rays / cpu_s / 1e6), 1)}
 
 
 # ---------------------------------------------------------------------------
@@ -645,6 +794,7 @@ def run_batched(args, rank, ws, local, dist):
 
     space = {"k": (2, 4, 8), "order": ("scanline", "morton8"), "empty_run": (2, 4, 8), "refill": (0, 8)}
     best, allres = autotune.search(measure, space=space, reps=1)
+    _save_autotune("batched", allres)
     b = batch_for(best["k"], best["order"])
     b.set_tuning(empty_run=best["empty_run"], persistent=True, refill=best["refill"])
     _barrier(dist)
@@ -702,9 +852,9 @@ def run_batched(args, rank, ws, local, dist):
         plain_pass()
     plain_ms = _max_over_ranks((time.perf_counter() - t0) * 1e3 / reps, dist)
     if rank != 0:
-        return
+        return None
     rays_all = rays_total * ws
-    print(json.dumps({
+    return ({
         "metric": "Mrays/s (64-scene batch: build + trace)", "value": round(rays_all / batched_ms / 1e3, 3),
         "unit": "Mrays/s", "n_gpus": ws, "steps": reps, "warmup": args.warmup, "ms_per_step": round(batched_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -714,8 +864,7 @@ def run_batched(args, rank, ws, local, dist):
                   "how": "per scene: rtg_scene_build (synchronous) + rtg_trace_nearest_device, 64 in sequence"},
         "batched_over_plain": round(plain_ms / batched_ms, 3),
         "breakdown_ms": {k_: round(v_, 4) for k_, v_ in breakdown.items()},
-        "autotune": [(c, round(m, 4)) for c, m in allres],
-    }), flush=True)
+    })
 
 
 # ---------------------------------------------------------------------------
@@ -799,6 +948,7 @@ def run_skewed(args, rank, ws, local, dist):
                  "heavy_cell": (0, 24, 48), "heavy_lanes": (16, 32), "cell_records": (False, True),
                  "refill": (0, 16)}
         best, allres = autotune.search(measure, space=space, reps=2)
+        _save_autotune("skewed", allres)
     _apply_tuning(s, best)
     k, order = best["k"], best["order"]
     for w in range(args.warmup):
@@ -857,9 +1007,9 @@ def run_skewed(args, rank, ws, local, dist):
     err = {"primary": _fp64_errors(sc.verts, sc.idx, prim_rays, prim),
            "secondary": _fp64_errors(sc.verts, sc.idx, sec_rays, sec)}
     if rank != 0:
-        return
+        return None
     clocks = sampler.summary() if sampler else {}
-    print(json.dumps({
+    return ({
         "metric": "Mrays/s (primary + diffuse secondary, grid build included)",
         "value": round(rays / t_ms / 1e3, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_ms / args.steps, 4), "higher_is_better": True,
@@ -878,10 +1028,9 @@ def run_skewed(args, rank, ws, local, dist):
                      "alg_bytes_per_launch": int(alg_bytes)},
         "fp64_error": err,
         "gpu_launches": int(lc1 - lc0),
-        "autotune": [(c, round(m, 4)) for c, m in allres],
         "clocks": {"sm_mhz": clocks.get("sm_mhz"), "sm_max_mhz": clocks.get("sm_max_mhz"),
                    "reasons": clocks.get("reasons", []), "samples": clocks.get("samples", 0)},
-    }), flush=True)
+    })
 
 
 # ---------------------------------------------------------------------------
@@ -964,9 +1113,9 @@ def run_instances(args, rank, ws, local, dist):
     t_flat = timed(lambda: flat.trace_nearest_device(d_rays, n, d_hits, stream=stream.cuda_stream))
     rays_all = _sum_over_ranks(n * args.steps, dist)
     if rank != 0:
-        return
+        return None
     tris_inst = sum(base[b].ntris for b, _, _ in inst)
-    print(json.dumps({
+    return ({
         "metric": "Mrays/s (two-level instanced closest hit)", "value": round(rays_all / t_inst / 1e6, 3),
         "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * t_inst / args.steps, 4), "higher_is_better": True, "scaling": "weak",
@@ -978,7 +1127,7 @@ def run_instances(args, rank, ws, local, dist):
         "flattened": {"value": round(rays_all / t_flat / 1e6, 3), "unit": "Mrays/s",
                       "ms_per_step": round(1e3 * t_flat / args.steps, 4),
                       "how": "all instances' triangles taken to world space in one scene, one-level trace"},
-    }), flush=True)
+    })
 
 
 # ---------------------------------------------------------------------------
@@ -1034,8 +1183,8 @@ def run_render(args, rank, ws, local, dist):
     total = _max_over_ranks(total, dist)
     rays_all = _sum_over_ranks(rays, dist)
     if rank != 0:
-        return
-    print(json.dumps({
+        return None
+    return ({
         "metric": "Mrays/s (shading wavefront: primary + shadow + reflected + refracted)",
         "value": round(rays_all / total / 1e6, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 4), "higher_is_better": True,
@@ -1043,7 +1192,7 @@ def run_render(args, rank, ws, local, dist):
         "config": {"workload": "render_plane_and_debris_1024x1024_depth3", "k": 4, "rays_per_step": rays // args.steps,
                    "timing": "host clock around the synchronous rtg_render call (per-level count read-backs "
                              "included); L2 flushed before each frame, outside the timed call"},
-    }), flush=True)
+    })
 
 
 # ---------------------------------------------------------------------------
@@ -1116,7 +1265,7 @@ def run_serving(args, rank, ws, local, dist):
     wu = make_requests(None, 20, 1)
     run(wu, False)
     run(wu, True)
-    rates = [10, 100, 1000, 2000]
+    rates = [int(r) for r in args.serve_rates.split(",") if r]
     out = {}
     for rate in rates:
         count = int(min(10_000, rate * args.serve_seconds))
@@ -1154,8 +1303,8 @@ def run_serving(args, rank, ws, local, dist):
                                            "over all of them (no copies, no request loop)"}
     del ceil_batch, tasks, d_src
     if rank != 0:
-        return
-    print(json.dumps({
+        return None
+    return ({
         "metric": "Mrays/s at saturation (served) + p50/p99 latency", "value": saturation["served"]["mrays_s"],
         "unit": "Mrays/s", "n_gpus": ws, "steps": len(rates), "warmup": 1, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -1169,7 +1318,7 @@ def run_serving(args, rank, ws, local, dist):
         "served_over_plain_pipelined": round(saturation["served"]["mrays_s"] /
                                              saturation["plain_pipelined"]["mrays_s"], 3),
         "rates": out,
-    }), flush=True)
+    })
 
 
 def _parse_tuning(text):
@@ -1191,37 +1340,151 @@ def _apply_tuning(scene, cfg):
                      cell_records=cfg.get("cell_records", False), refill=cfg.get("refill", 0))
 
 
+def _tune_str(cfg) -> str:
+    """A launch-shape choice in a few characters: order/ER/persistent/heavy
+    cell x lanes/refill/cell records."""
+    if not cfg:
+        return ""
+    return (f"{cfg.get('order', '')}/er{cfg.get('empty_run', '')}/p{int(bool(cfg.get('persistent', 0)))}"
+            f"/h{cfg.get('heavy_cell', 0)}x{cfg.get('heavy_lanes', 32)}/r{cfg.get('refill', 0)}"
+            f"/c{int(bool(cfg.get('cell_records', 0)))}")
+
+
+def _r(x, n=3):
+    return None if x is None else round(float(x), n)
+
+
+def compact_line(full: dict, subs: dict) -> dict:
+    """The one result line: the headline workload's contract keys and
+    figures, then one small object per further workload (about 2.5 KB in
+    all; every figure of the sub-objects is in Mrays/s or ms as its key
+    says; everything else goes to --detail)."""
+    c = {k: full[k] for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                              "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
+    cfg = full["config"]
+    c["config"] = {"workload": cfg["workload"], "k": cfg["k"], "frames": cfg["frames"], "triangles": cfg["triangles"],
+                   "rays_primary": cfg["rays_primary"], "l2": "flushed between frames (256 MiB write)",
+                   "parallelism": cfg["parallelism"], "tuning": _tune_str(cfg["tuning"]),
+                   "tuned_by": full.get("autotune", {}).get(str(cfg["k"]), {}).get("source")}
+    c["build_ms"] = _r(full["build_ms"], 4)
+    c["trace_mrays_s"] = _r(full["trace_mrays_s"], 1)
+    c["per_k"] = {k: {"value": _r(v["value"], 1), "build_ms": _r(v["build_ms"], 4),
+                      "stream_value": _r(v["stream_value"], 1)} for k, v in full["per_k"].items()}
+    rf = full["roofline"]
+    c["roofline"] = {"bound": rf["bound"], "achieved": rf["achieved"], "peak": rf["peak"], "unit": rf["unit"],
+                     "frac": rf["frac"], "traffic": rf["traffic"], "peak_source": rf["peak_source"],
+                     "kernel": "trace_kernel frame + deferred pass", "kernel_ms": rf["kernel_ms"],
+                     "alg_bytes": rf["alg_bytes_per_launch"], "l2_frac": rf["l2"]["frac"], "l2_peak": rf["l2"]["peak"]}
+    br = full["build_roofline"]
+    c["build_roofline"] = {"achieved": br["achieved"], "frac": br["frac"], "alg_bytes": br["alg_bytes"],
+                           "ms": _r(br["ms"], 4)}
+    cb = full["cpu_baseline"]
+    c["cpu_baseline"] = {"value": cb["value"], "unit": cb["unit"], "cores": cb["cores"], "kind": cb["kind"],
+                         "sample": f"10 frames k={cfg['k']}, every ray", "build_ms": cb["build_ms"]}
+    e = full["e2e"]
+    c["e2e"] = {"value": e["value"], "unit": e["unit"], "h2d_bytes_per_step": e["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": e["d2h_bytes_per_step"], "ms_per_step": e["ms_per_step"]}
+    c["gpu_launches"] = full["gpu_launches"]
+    ck = full["clocks"]
+    c["clocks"] = {"sm_mhz": ck["sm_mhz"], "sm_max_mhz": ck["sm_max_mhz"], "reasons": ck["reasons"]}
+    for name, sub in subs.items():
+        c[name] = sub
+    return c
+
+
+def compact_skewed(d: dict) -> dict:
+    if d is None or "error" in d:
+        return d
+    err = d["fp64_error"]
+    return {"workload": "skewed_1048576tri_1024x1024_diffuse", "k": d["config"]["k"], "value": _r(d["value"], 1),
+            "ms_per_step": d["ms_per_step"], "build_ms": d["build_ms"], "trace_ms": d["trace_ms"],
+            "rays_per_step": d["config"]["rays_per_step"], "tests_per_ray": d["counters"]["tests_per_ray"],
+            "roofline_frac": d["roofline"]["frac"], "tuning": _tune_str(d["config"]["tuning"]),
+            "fp64_max": {g: [_r(err[g]["t_rel"]["max"], 8), _r(err[g]["u_abs"]["max"], 8),
+                             _r(err[g]["v_abs"]["max"], 8)] for g in ("primary", "secondary")}}
+
+
+def compact_batched(d: dict) -> dict:
+    if d is None or "error" in d:
+        return d
+    b = d["breakdown_ms"]
+    return {"workload": "batched_64_scenes", "value": _r(d["value"], 1), "plain": _r(d["plain"]["value"], 1),
+            "ratio": d["batched_over_plain"], "ms_per_step": d["ms_per_step"], "plain_ms": d["plain"]["ms_per_step"],
+            "build_ms": _r(b["batched_build_ms"], 3), "trace_ms": _r(b["batched_trace_ms"], 3),
+            "tuning": "k{k}/{order}/er{empty_run}/r{refill}".format(**d["config"]["tuning"])}
+
+
+def compact_serving(d: dict) -> dict:
+    if d is None or "error" in d:
+        return d
+    sat = d["saturation"]
+    out = {"workload": "serving_16_scenes", "value": sat["served"]["mrays_s"], "plain": sat["plain"]["mrays_s"],
+           "ratio": d["served_over_plain"], "p50_ms": sat["served"]["p50_ms"], "p99_ms": sat["served"]["p99_ms"],
+           "plain_p50_ms": sat["plain"]["p50_ms"], "plain_p99_ms": sat["plain"]["p99_ms"],
+           "requests": sat["served"]["requests"], "device_ceiling": sat["device_ceiling"]["mrays_s"]}
+    for rate, r in d["rates"].items():
+        out[f"r{rate}"] = {"p50_ms": r["served"]["p50_ms"], "p99_ms": r["served"]["p99_ms"],
+                           "plain_p50_ms": r["plain"]["p50_ms"], "plain_p99_ms": r["plain"]["p99_ms"],
+                           "requests": r["served"]["requests"]}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
-    ap.add_argument("--workload", default="deforming",
-                    choices=["deforming", "batched", "serving", "skewed", "instances", "render"])
+    ap.add_argument("--workload", default="default",
+                    choices=["default", "deforming", "plain", "batched", "serving", "skewed", "instances", "render"],
+                    help="default: the deforming-mesh headline plus the plain, skewed, batched and serving "
+                         "workloads in one line; any other: that workload alone, in full")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
+    ap.add_argument("--serve-rates", default="10,100,1000,2000")
     ap.add_argument("--serve-refill", type=int, default=8,
                     help="lane-refill threshold of the serving scenes (served and plain paths alike)")
     ap.add_argument("--fixed-tuning", default="",
                     help="skip the autotuner: e.g. k=8,order=morton8,empty_run=4,persistent=0 (profiling runs)")
+    ap.add_argument("--detail", default="", help="also write every workload's full result to this JSON file")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, ws, local, dist = _dist()
+    single = {"plain": run_plain_small, "batched": run_batched, "serving": run_serving, "skewed": run_skewed,
+              "instances": run_instances, "render": run_render}
+    detail = {}
     if args.impl == "reference":
-        run_reference(args, rank, ws, dist)
-    elif args.workload == "batched":
-        run_batched(args, rank, ws, local, dist)
-    elif args.workload == "serving":
-        run_serving(args, rank, ws, local, dist)
-    elif args.workload == "skewed":
-        run_skewed(args, rank, ws, local, dist)
-    elif args.workload == "instances":
-        run_instances(args, rank, ws, local, dist)
-    elif args.workload == "render":
-        run_render(args, rank, ws, local, dist)
+        line = run_reference(args, rank, ws, dist)
+    elif args.workload in single:
+        line = single[args.workload](args, rank, ws, local, dist)
+        detail[args.workload] = line
     else:
-        run_gpu(args, rank, ws, local, dist)
+        full = run_gpu(args, rank, ws, local, dist)
+        detail["deforming"] = full
+        subs = {}
+        if args.workload == "default" and ws == 1:
+            import argparse as _ap
+            import torch
+            serve_args = _ap.Namespace(**vars(args))
+            serve_args.serve_rates, serve_args.serve_seconds, serve_args.serve_saturation = "1000", 3.0, 2000
+            for name, fn, squash in (("cfg0_plain", run_plain_small, None),
+                                     ("cfg2_skewed", run_skewed, compact_skewed),
+                                     ("cfg3_batched", run_batched, compact_batched),
+                                     ("cfg4_serving", run_serving, compact_serving)):
+                try:
+                    d = fn(serve_args if name == "cfg4_serving" else args, rank, ws, local, dist)
+                    detail[name] = d
+                    subs[name] = squash(d) if squash else d
+                except Exception as exc:          # one workload's failure keeps the headline line
+                    subs[name] = {"error": f"{type(exc).__name__}: {exc}"[:160]}
+                torch.cuda.synchronize()
+                torch.cuda.empty_cache()
+        line = compact_line(full, subs) if full is not None else None
+    if rank == 0 and line is not None:
+        if args.detail:
+            with open(args.detail, "w") as f:
+                json.dump(detail, f, indent=1, default=str)
+        print(json.dumps(line, separators=(",", ":")), flush=True)
     if dist is not None:
         dist.destroy_process_group()
 

@@ -18,10 +18,12 @@
 // on the GPU -- on different streams, or from different host threads at once
 // -- race on the array.  Serialise them (one stream, or wait between calls).
 //
-// Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current, and sets the large-cell
-// sort kernel's shared-memory limit.  Make that first call before any stream
-// capture begins on the device.
+// Set-up: every call looks up the array's device address with
+// cudaGetSymbolAddress on the device that is current, and sets the large-cell
+// sort kernel's shared-memory limit there (so a call after cudaDeviceReset
+// finds the new context's address); the first call on a device also reads
+// its SM count and shared-memory limit.  Make that first call before any
+// stream capture begins on the device.
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -85,23 +87,29 @@ rtg_status setup_device(int dev, DeviceSetup** out) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     DeviceSetup& d = g_setup[dev];
     if (!d.ready) {
-        void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_arena);
-        if (e != cudaSuccess || !ptr) return failure(RTG_DEVICE_ERROR, "cudaGetSymbolAddress(arena)", e);
         int sms = 0, optin = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess) return failure(RTG_DEVICE_ERROR, "SM count", e);
         e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (e != cudaSuccess) return failure(RTG_DEVICE_ERROR, "shared-memory limit", e);
         int words = 32768;
         while (words * 4 + 4096 > optin && words > 1024) words >>= 1;
-        e = build_setup_attributes(words);
-        if (e != cudaSuccess) return failure(RTG_DEVICE_ERROR, "large-cell sort attribute", e);
-        d.arena = static_cast<unsigned char*>(ptr);
         d.num_sms = sms;
         d.bitmap_words = words;
         d.ready = true;
     }
+    // The array's address and the large-cell sort's shared-memory limit
+    // belong to the device's current context: a device reset
+    // (cudaDeviceReset) gives the next call a new context, in which the
+    // array may sit elsewhere and the kernel's attribute is back at its
+    // default.  So every call looks the address up again and re-applies the
+    // attribute (both host-side calls of a few microseconds).
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_arena);
+    if (e != cudaSuccess || !ptr) return failure(RTG_DEVICE_ERROR, "cudaGetSymbolAddress(arena)", e);
+    e = build_setup_attributes(d.bitmap_words);
+    if (e != cudaSuccess) return failure(RTG_DEVICE_ERROR, "large-cell sort attribute", e);
+    d.arena = static_cast<unsigned char*>(ptr);
     *out = &d;
     return RTG_OK;
 }

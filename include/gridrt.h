@@ -238,9 +238,11 @@ rtg_status rtg_trace_frame_wait(rtg_scene scene, uint64_t ticket);
  * 16,777,216 cells per call; larger grids return RTG_INVALID_PARAM.  The call
  * synchronises `stream` before returning.  All calls share that array: each
  * call clears what must start from zero, and calls that overlap on the GPU
- * (different streams or threads at once) race -- serialise them.  The first
- * call on a device looks up the array's address (cudaGetSymbolAddress) with
- * that device current; make it before any stream capture on that device. */
+ * (different streams or threads at once) race -- serialise them.  Every
+ * call looks up the array's address (cudaGetSymbolAddress) on the device that
+ * is current, so calls after a device reset use the new context's array; the
+ * first call on a device also reads the device's limits -- make it before any
+ * stream capture on that device. */
 rtg_status rtg_grid_build_noalloc(const float* d_verts, int64_t nverts, const int32_t* d_tris, int64_t ntris,
                                   int32_t k, int32_t* d_offsets, int64_t offsets_cap, int32_t* d_ids,
                                   int64_t ids_cap, float* d_tri_records, rtg_grid_info* info, void* stream);
@@ -376,9 +378,12 @@ rtg_status rtg_render(rtg_scene scene, const rtg_camera* cam, const rtg_shading*
                       int64_t* rays_out, void* stream);
 
 /* ---- measurement ----------------------------------------------------------
- * Read bandwidth of this device over a buffer of `bytes` (16-byte loads that
- * bypass L1, `reps` passes, best of 5 timed launches): a buffer well inside L2
- * measures L2, one far above it HBM.  Allocates and frees the buffer. */
+ * Public diagnostic: the read bandwidth of this device over a buffer of
+ * `bytes` (16-byte loads that bypass L1, `reps` passes, best of 5 timed
+ * launches).  A buffer well inside L2 measures L2, one far above it HBM; a
+ * caller uses it as the denominator of a trace's bandwidth fraction on the
+ * machine at hand.  Allocates and frees the buffer; not for use while the
+ * device runs other timed work. */
 rtg_status rtg_probe_read_gbs(int32_t device, int64_t bytes, int32_t reps, double* gbs);
 
 /* ---- two-level instancing -------------------------------------------------

@@ -20,7 +20,20 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "liboracle_ref.so")
-REF_SRC = os.environ.get("GRIDRT_REFERENCE_DIR", "/root/reference")
+
+
+def reference_dir() -> str:
+    """The reference checkout: GRIDRT_REFERENCE_DIR when set, else the build
+    recipe's default (oracle/Makefile, `make print-ref`).  May not exist."""
+    env = os.environ.get("GRIDRT_REFERENCE_DIR")
+    if env:
+        return env
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True, timeout=60)
+        return out.stdout.strip()
+    except Exception:
+        return ""
+
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -44,8 +57,9 @@ def build(ref: bool = False) -> None:
     """Compile liboracle.so (and, with ref=True, the compiled reference when its
     sources are present)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    if ref and os.path.isdir(os.path.join(REF_SRC, "src", "rtplugins")):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"])
+    ref_src = reference_dir() if ref else ""
+    if ref_src and os.path.isdir(os.path.join(ref_src, "src", "rtplugins")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref_src}"])
 
 
 _lib = None

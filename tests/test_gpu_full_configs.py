@@ -1,0 +1,127 @@
+"""Parity at the workloads' full sizes: every ray of the benchmark
+configurations against the oracle, not a subsample.
+
+* deforming sphere (102,400 triangles): one frame at 1024 x 1024 for each
+  k in {2, 4, 8} -- grid bits, every primary ray's closest hit, and the
+  occlusion of every shadow ray the frame call wrote;
+* skewed density (1,048,576 triangles, k = 8): every 1024 x 1024 primary ray
+  and every diffuse secondary ray generated from their hits on the device;
+* the 64-scene uneven batch: the whole batch built and traced in one batch
+  launch, eight of its scenes (the largest, the smallest and six between)
+  compared with the oracle directly, ray for ray.
+
+Closest hits follow the near-tie rules of parity.py (same triangle: t / u / v
+within 1e-5 relative; different triangle only at a documented near-tie), and
+shadow-ray disagreements must each be explained by the occluding triangle."""
+import numpy as np
+import pytest
+
+import parity
+from gridrt import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _report(name, st):
+    print(f"\n[{name}] " + ", ".join(f"{k}={v}" for k, v in st.items()
+                                     if k not in ("unexplained_examples", "fp64")))
+
+
+@pytest.mark.parametrize("k", [2, 4, 8])
+def test_deforming_sphere_full_frame(gridlib, oracle, k):
+    import torch
+    sc = scenes.deforming_sphere(7)
+    s = gridlib.Scene(0)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(k)
+    g = oracle.Grid(sc.verts, sc.idx, k)
+    off, ids = s.download()
+    assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
+    cam = scenes.deforming_sphere_camera(1024, 1024)
+    n = cam.width * cam.height
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    s.trace_frame_device(cam, scenes.SPHERE_LIGHT, d_hits, d_occ, d_sr, order="morton8")
+    torch.cuda.synchronize()
+    rays = scenes.camera_rays(cam, "morton8")
+    gh = gridlib.split_hits(d_hits.cpu().numpy())
+    oh = g.trace_closest(rays)
+    st = parity.compare_hits(gh, oh, sc.verts, sc.idx, rays, oracle)
+    _report(f"sphere 1024^2 k={k}", st)
+    parity.assert_parity(st)
+    sr = d_sr.cpu().numpy()
+    occ = d_occ.cpu().numpy()
+    has = sr[:, 7] >= 0
+    assert (occ[~has] == 2).all()
+    srh = np.ascontiguousarray(sr[has])
+    parity.check_occlusion(f"sphere 1024^2 k={k}", s, g, gridlib.split_hits, srh, occ[has], g.trace_any(srh),
+                           sc.verts, sc.idx, oracle)
+
+
+def test_skewed_density_full(gridlib, oracle):
+    import torch
+    k = 8
+    sc = scenes.skewed_density()
+    s = gridlib.Scene(0)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(k)
+    g = oracle.Grid(sc.verts, sc.idx, k)
+    off, ids = s.download()
+    assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
+    cam = scenes.skewed_density_camera(1024, 1024)
+    n = cam.width * cam.height
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    d_sec = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    d_hits2 = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    s.trace_camera_diffuse_device(cam, 4242, d_hits, d_sec, order="morton8")
+    s.trace_nearest_device(d_sec, n, d_hits2)
+    torch.cuda.synchronize()
+    rays = scenes.camera_rays(cam, "morton8")
+    st = parity.compare_hits(gridlib.split_hits(d_hits.cpu().numpy()), g.trace_closest(rays), sc.verts, sc.idx,
+                             rays, oracle)
+    _report("skewed 1024^2 primary", st)
+    parity.assert_parity(st)
+    sec = d_sec.cpu().numpy()
+    has = sec[:, 7] > 0
+    sec_rays = np.ascontiguousarray(sec[has])
+    sh = gridlib.split_hits(d_hits2.cpu().numpy()[has])
+    st = parity.compare_hits(sh, g.trace_closest(sec_rays), sc.verts, sc.idx, sec_rays, oracle)
+    _report("skewed diffuse secondary", st)
+    parity.assert_parity(st)
+
+
+def test_batched_workload_against_oracle(gridlib, oracle):
+    import torch
+    items = scenes.batched_workload()
+    scs, tasks, outs = [], [], []
+    for i, it in enumerate(items):
+        s = gridlib.Scene(0)
+        s.set_geometry(it.scene.verts, it.scene.idx)
+        scs.append(s)
+        d_rays = torch.from_numpy(it.rays).cuda()
+        out = torch.empty((it.rays.shape[0], 4), dtype=torch.int32, device="cuda")
+        tasks.append((i, gridlib.RTG_MODE_NEAREST, d_rays, it.rays.shape[0], out))
+        outs.append(out)
+    b = gridlib.Batch(scs, [4] * len(items), tasks)
+    b.build_async()
+    b.trace_async()
+    assert b.check() == 0
+    torch.cuda.synchronize()
+    sizes = np.array([it.scene.ntris for it in items])
+    order = np.argsort(sizes)
+    pick = sorted(set([int(order[0]), int(order[-1])] + [int(order[j]) for j in np.linspace(1, len(items) - 2, 6)
+                                                         .round().astype(int)]))
+    assert len(pick) == 8
+    total = 0
+    for i in pick:
+        it = items[i]
+        g = oracle.Grid(it.scene.verts, it.scene.idx, 4)
+        off, ids = scs[i].download()
+        assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids), i
+        st = parity.compare_hits(gridlib.split_hits(outs[i].cpu().numpy()), g.trace_closest(it.rays),
+                                 it.scene.verts, it.scene.idx, it.rays, oracle)
+        _report(f"batch scene {i} ({it.scene.ntris} tris)", st)
+        parity.assert_parity(st)
+        total += it.rays.shape[0]
+    print(f"\n[batch] {len(pick)} scenes, {total} rays against the oracle")

@@ -108,3 +108,67 @@ def test_noalloc_rejects_grids_over_its_limit(gridlib):
     rc = L.rtg_grid_build_noalloc(d_verts.data_ptr(), sc.nverts, d_tris.data_ptr(), sc.ntris, 4, off.data_ptr(),
                                   off.numel(), ids.data_ptr(), ids.numel(), rec.data_ptr(), ctypes.byref(info), None)
     assert rc == gridlib.RTG_INVALID_PARAM and info.nrefs > (1 << 19)
+    # the shared working array is usable straight after the rejected call
+    good = scenes.plane_and_debris(quads=48, debris=4096)
+    _check_against_regular(gridlib, L, good.verts, good.idx, 4)
+
+
+def _check_against_regular(gridlib, L, verts, idx, k):
+    info_a, off_a, ids_a, rec = _noalloc_build(gridlib, L, verts, idx, k)
+    info_b, off_b, ids_b = _regular_build(gridlib, verts, idx, k)
+    assert info_a["res"] == info_b["res"] and info_a["nrefs"] == info_b["nrefs"]
+    for key in ("bmin", "bmax", "cell", "inv_cell"):
+        assert np.array_equal(info_a[key].view(np.uint32), info_b[key].view(np.uint32)), key
+    assert np.array_equal(off_a, off_b), "offsets differ from rtg_scene_build"
+    assert np.array_equal(ids_a, ids_b), "sorted cell lists differ from rtg_scene_build"
+    assert np.array_equal(rec.view(np.uint32), _expected_records(verts, idx).view(np.uint32))
+    return info_a, off_a, ids_a
+
+
+def _resolution_is_ambiguous(verts, ntris, k):
+    """The device's test, restated in float32: the grid box enlarged by 1%
+    (Aabb::scaleBy), V, k * N / V, f = pow(q, 1/3) rounded from double, and
+    whether ceil(extent * f) changes between f - 1 ulp and f + 1 ulp on some
+    axis (then the host's powf decides the resolution)."""
+    f32 = np.float32
+    mn, mx = verts.min(0).astype(f32), verts.max(0).astype(f32)
+    s = np.where(mn == mx, f32(0.01), (np.abs(mx - mn) * f32(0.01)).astype(f32)).astype(f32)
+    mn, mx = (mn - s).astype(f32), (mx + s).astype(f32)
+    d = (mx - mn).astype(f32)
+    V = f32(f32(d[0] * d[1]) * d[2])
+    q = f32(f32(k * ntris) / V)
+    f = f32(np.float64(q) ** np.float64(f32(1.0) / f32(3.0)))
+    fm, fp = np.nextafter(f, f32(0.0)), np.nextafter(f, f32(np.inf))
+    return bool((np.ceil((d * fm).astype(f32)) != np.ceil((d * fp).astype(f32))).any())
+
+
+def _ambiguous_scene(k=4, n=200, seed=5):
+    """A soup of n small triangles in the unit cube plus one triangle
+    (0,0,0), (0.5,1,1), (X,0.5,0.5) whose x extent X is chosen, by search over
+    float32 values, so that the resolution rule sits on a powf ulp boundary."""
+    rng = np.random.default_rng(seed)
+    cent = rng.uniform(0.05, 0.95, size=(n, 3)).astype(np.float32)
+    soup = (cent[:, None, :] + rng.uniform(-0.03, 0.03, size=(n, 3, 3))).astype(np.float32).reshape(-1, 3)
+    for i in range(2_000_000):
+        X = np.float32(1.0 + 1e-6 * i)
+        verts = np.concatenate([soup, np.array([[0, 0, 0], [0.5, 1, 1], [X, 0.5, 0.5]], np.float32)])
+        if _resolution_is_ambiguous(verts, n + 1, k):
+            idx = np.arange(3 * (n + 1), dtype=np.int32).reshape(-1, 3)
+            return verts, idx
+    raise AssertionError("no ambiguous extent found")
+
+
+def test_noalloc_host_resolved_parameters(gridlib, oracle):
+    """A scene whose resolution depends on the last ulp of powf takes the
+    path where the call re-resolves the parameters on the host and clears
+    the sort counters in the shared array by hand: the grid still equals
+    rtg_scene_build's and the oracle's, also on a second call in a row."""
+    L = gridlib.load()
+    verts, idx = _ambiguous_scene()
+    for _ in range(2):
+        info, off, ids = _check_against_regular(gridlib, L, verts, idx, 4)
+        g = oracle.Grid(verts, idx, 4)
+        assert np.array_equal(off, g.offsets) and np.array_equal(ids, g.ids)
+    # and an ordinary build right after it
+    sc = scenes.plane_and_debris(quads=40, debris=3000)
+    _check_against_regular(gridlib, L, sc.verts, sc.idx, 4)
