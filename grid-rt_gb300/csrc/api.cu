@@ -318,6 +318,9 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
         ok = ok && cudaEventCreateWithFlags(&s->fork.fork, cudaEventDisableTiming) == cudaSuccess;
         ok = ok && cudaEventCreateWithFlags(&s->fork.join[0], cudaEventDisableTiming) == cudaSuccess;
         ok = ok && cudaEventCreateWithFlags(&s->fork.join[1], cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaStreamCreateWithFlags(&s->fork.rec, cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&s->fork.rec_fork, cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&s->fork.rec_join, cudaEventDisableTiming) == cudaSuccess;
         s->have_fork = ok;
         if (!ok) cudaGetLastError();
     }
@@ -372,6 +375,12 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
         if (s->fork.join[i]) cudaEventDestroy(s->fork.join[i]);
     }
     if (s->fork.fork) cudaEventDestroy(s->fork.fork);
+    if (s->fork.rec) {
+        cudaStreamSynchronize(s->fork.rec);
+        cudaStreamDestroy(s->fork.rec);
+    }
+    if (s->fork.rec_fork) cudaEventDestroy(s->fork.rec_fork);
+    if (s->fork.rec_join) cudaEventDestroy(s->fork.rec_join);
     cudaFree(s->d_fring);
     for (int i = 0; i < 2; ++i) {
         if (s->frame_traced[i]) cudaEventDestroy(s->frame_traced[i]);

@@ -7,19 +7,24 @@
 // offsets[ncells + 1] and ids[nrefs], each cell's list sorted by triangle id,
 // bit-identical to the reference's per-cell std::vector lists.
 //
-// Pipeline (all on one stream, no host round trip):
+// Pipeline (no host round trip):
+//   records       the trace's triangle records: Moller-Trumbore {v0|id, e1,
+//                 e2} and the reference's TriAccel record (on a stream of its
+//                 own beside the passes below, joined at the end)
 //   bbox_params   scene box (exact min/max), 1% enlargement, resolution rule;
-//                 the last block derives the grid parameters on the device
-//   zero_offsets  clears offsets[0..ncells]
+//                 the last block derives the grid parameters on the device;
+//                 also clears the offsets and the occupancy bitmap
+//   zero_offsets  the clear alone (host-resolved parameters)
 //   count         warp-cooperative expansion of each triangle's cell range;
-//                 warp-aggregated atomicAdd of per-cell counts; writes the
-//                 Moller-Trumbore triangle records {v0|id, e1, e2}
-//   scan x3       in-place inclusive scan of the counts (cursors = cell ends)
+//                 warp-aggregated atomicAdd of per-cell counts
+//   scan x2       tile sums, then the in-place inclusive scan of the counts
+//                 (cursors = cell ends), occupancy bits and the sort queues
 //   scatter       same expansion; warp-aggregated atomicSub on the cursors,
 //                 which leaves them equal to the exclusive cell starts
-//   sort x3       per-cell sort by triangle id: warp bitonic (<= 32), block
-//                 bitonic in shared memory (<= 4096), shared-memory bitmap
-//                 compaction for larger cells (ids within a cell are unique)
+//   sort x3       per-cell sort by triangle id: thread network (<= 8), warp
+//                 bitonic (<= 256), block bitonic in shared memory (<= 4096),
+//                 shared-memory bitmap compaction for larger cells (ids
+//                 within a cell are unique)
 #include "common.cuh"
 #include "kernels.h"
 
@@ -305,11 +310,10 @@ __device__ __forceinline__ float3 load_vert(const float* __restrict__ verts, int
 
 // Enumerates every (cell, triangle) reference of the warp's 32 triangles, 32
 // references per step, and calls emit(cell, tri, active) on every lane.
-template <bool WRITE_TRIS, class Emit>
+template <class Emit>
 __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restrict__ verts,
                                             const int32_t* __restrict__ idx, int64_t ntris, int64_t base,
-                                            float4* __restrict__ tris, float4* __restrict__ wald, GridParams* p,
-                                            BuildWork* w, Emit&& emit) {
+                                            GridParams* p, BuildWork* w, Emit&& emit) {
     const int lane = threadIdx.x & 31;
     const int64_t t = base + lane;
     int32_t lo[3] = {0, 0, 0}, ext[3] = {1, 1, 1};
@@ -330,12 +334,6 @@ __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restri
         } else {
             raise_status(p, w, ST_BAD_RANGE);
             ext[0] = ext[1] = ext[2] = 1;
-        }
-        if (WRITE_TRIS) {
-            tris[3 * t + 0] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int32_t)t));
-            tris[3 * t + 1] = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.0f);
-            tris[3 * t + 2] = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.0f);
-            if (wald) write_wald_record(wald + 3 * t, v0, v1, v2, (int32_t)t);
         }
     }
     unsigned long long incl = cnt;
@@ -374,9 +372,8 @@ __device__ __forceinline__ void warp_expand(const Lite& L, const float* __restri
 }
 
 __device__ __forceinline__ void count_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
-                                                    int64_t ntris, GridParams* p, BuildWork* w,
-                                                    int32_t* __restrict__ counts, float4* __restrict__ tris,
-                                                    float4* __restrict__ wald, unsigned vbx, unsigned vgx) {
+                                           int64_t ntris, GridParams* p, BuildWork* w,
+                                           int32_t* __restrict__ counts, unsigned vbx, unsigned vgx) {
     if (fatal(p->status)) return;
     Lite L;
     load_lite(p, L);
@@ -384,7 +381,7 @@ __device__ __forceinline__ void count_body(const float* __restrict__ verts, cons
     const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
-        warp_expand<true>(L, verts, idx, ntris, base, tris, wald, p, w, [&](int32_t cell, int32_t, bool active) {
+        warp_expand(L, verts, idx, ntris, base, p, w, [&](int32_t cell, int32_t, bool active) {
             const unsigned peers = __match_any_sync(FULL, cell);
             const int leader = __ffs(peers) - 1;
             if (active && lane == leader) atomicAdd(&counts[cell], __popc(peers));
@@ -399,11 +396,11 @@ __global__ void __launch_bounds__(256) count_kernel(BuildArgs one, const BuildAr
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
-        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, a.wald, blockIdx.x - (unsigned)first[t],
+        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, blockIdx.x - (unsigned)first[t],
                    (unsigned)(first[t + 1] - first[t]));
     } else {
         const BuildArgs& a = one;
-        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, a.tris, a.wald, blockIdx.x, gridDim.x);
+        count_body(a.verts, a.idx, a.ntris, a.params, a.work, a.offsets, blockIdx.x, gridDim.x);
     }
 }
 
@@ -1034,17 +1031,19 @@ __global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const B
 }
 
 // Triangle records in cell-list order: crec[3i..3i+2] = tris[3 ids[i] ..].
+// One float4 a thread: thread q copies component q % 3 of the record of
+// list entry q / 3, so a warp's stores cover 512 contiguous bytes (storing a
+// whole record a thread left each store instruction 48 bytes apart a lane).
 __device__ __forceinline__ void cell_records_body(const int32_t* __restrict__ ids, const float4* __restrict__ tris,
                                                   float4* __restrict__ crec, const GridParams* p, unsigned vbx,
                                                   unsigned vgx) {
     if (!crec || build_failed(p->status)) return;
-    const int64_t R = p->nrefs;
+    const int64_t Q = 3 * p->nrefs;
     const int64_t stride = (int64_t)vgx * blockDim.x;
-    for (int64_t i = (int64_t)vbx * blockDim.x + threadIdx.x; i < R; i += stride) {
-        const int64_t t = ids[i];
-        crec[3 * i] = __ldg(tris + 3 * t);
-        crec[3 * i + 1] = __ldg(tris + 3 * t + 1);
-        crec[3 * i + 2] = __ldg(tris + 3 * t + 2);
+    for (int64_t q = (int64_t)vbx * blockDim.x + threadIdx.x; q < Q; q += stride) {
+        const int64_t i = q / 3;
+        const int64_t t = __ldg(ids + i);
+        crec[q] = __ldg(tris + 3 * t + (q - 3 * i));
     }
 }
 
@@ -1059,6 +1058,38 @@ __global__ void __launch_bounds__(256) cell_records_kernel(BuildArgs one, const 
                           (unsigned)(first[t + 1] - first[t]));
     } else {
         cell_records_body(one.ids, one.tris, one.crec, one.params, blockIdx.x, gridDim.x);
+    }
+}
+
+// Triangle records, one triangle a thread: the trace's Moller-Trumbore record
+// {v0, id}, {v1 - v0, 0}, {v2 - v0, 0} and, when the scene keeps them, the
+// reference's TriAccel record.  Needs only the vertices and indices, so a
+// single-scene build runs it on a stream of its own beside the grid passes.
+__device__ __forceinline__ void records_body(const float* __restrict__ verts, const int32_t* __restrict__ idx,
+                                             int64_t ntris, float4* __restrict__ tris, float4* __restrict__ wald,
+                                             unsigned vbx, unsigned vgx) {
+    const int64_t stride = (int64_t)vgx * blockDim.x;
+    for (int64_t t = (int64_t)vbx * blockDim.x + threadIdx.x; t < ntris; t += stride) {
+        const int32_t i0 = __ldg(idx + 3 * t), i1 = __ldg(idx + 3 * t + 1), i2 = __ldg(idx + 3 * t + 2);
+        const float3 v0 = load_vert(verts, i0), v1 = load_vert(verts, i1), v2 = load_vert(verts, i2);
+        tris[3 * t + 0] = make_float4(v0.x, v0.y, v0.z, __int_as_float((int32_t)t));
+        tris[3 * t + 1] = make_float4(fsub(v1.x, v0.x), fsub(v1.y, v0.y), fsub(v1.z, v0.z), 0.0f);
+        tris[3 * t + 2] = make_float4(fsub(v2.x, v0.x), fsub(v2.y, v0.y), fsub(v2.z, v0.z), 0.0f);
+        if (wald) write_wald_record(wald + 3 * t, v0, v1, v2, (int32_t)t);
+    }
+}
+
+template <bool MULTI>
+__global__ void __launch_bounds__(256) records_kernel(BuildArgs one, const BuildArgs* __restrict__ many,
+                                                      const int* __restrict__ first, int ntasks) {
+    pdl_begin();
+    if (MULTI) {
+        const int t = block_task(first, ntasks);
+        const BuildArgs& a = many[t];
+        records_body(a.verts, a.idx, a.ntris, a.tris, a.wald, blockIdx.x - (unsigned)first[t],
+                     (unsigned)(first[t + 1] - first[t]));
+    } else {
+        records_body(one.verts, one.idx, one.ntris, one.tris, one.wald, blockIdx.x, gridDim.x);
     }
 }
 
@@ -1078,15 +1109,28 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     out[BK_SSMALL] = clampi(a.cell_cap / 512 + 1, 8 * sms);
     out[BK_SMED] = clampi(a.cell_cap / 2048 + 1, 4 * sms);             // 16 warps a block, one cell a warp
     out[BK_SLARGE] = clampi(a.cell_cap / 16384 + 1, 2 * sms);
-    out[BK_REFS] = a.crec ? clampi((a.ref_cap + 255) / 256, 16 * sms) : 0;
+    out[BK_REFS] = a.crec ? clampi((3 * a.ref_cap + 255) / 256, 16 * sms) : 0;
+    out[BK_RECS] = clampi((a.ntris + 255) / 256, 16 * sms);
 }
 
 template <bool MULTI>
 static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BatchGrid& g,
                               bool skip_bbox, int bitmap_words, cudaStream_t st, const BuildFork* fork = nullptr) {
-    count_launches(8);
+    count_launches(9);
     const int* f[kBuildKinds];
     for (int k = 0; k < kBuildKinds; ++k) f[k] = MULTI ? g.first[k] : nullptr;
+    // the triangle records: on the record stream beside the whole build (it
+    // starts after everything before the build on `st` -- the previous
+    // frame's traces, which read the records -- and the build's end waits
+    // for it), else first on `st`
+    const bool rec_side = fork && fork->rec;
+    if (rec_side) {
+        cudaEventRecord(fork->rec_fork, st);
+        cudaStreamWaitEvent(fork->rec, fork->rec_fork, 0);
+    }
+    launch_k(records_kernel<MULTI>, g.total[BK_RECS], 256, 0, rec_side ? fork->rec : st, one, many, f[BK_RECS],
+             ntasks);
+    if (rec_side) cudaEventRecord(fork->rec_join, fork->rec);
     // the box pass also clears the offsets and the bitmap; host-resolved
     // parameters skip it and clear them on their own
     if (!skip_bbox)
@@ -1117,6 +1161,7 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
         cudaStreamWaitEvent(st, fork->join[0], 0);
         cudaStreamWaitEvent(st, fork->join[1], 0);
     }
+    if (rec_side) cudaStreamWaitEvent(st, fork->rec_join, 0);
     if (g.total[BK_REFS] > 0) {
         count_launches(1);
         launch_k(cell_records_kernel<MULTI>, g.total[BK_REFS], 256, 0, st, one, many, f[BK_REFS], ntasks);

@@ -49,11 +49,16 @@ struct BuildFork {
     cudaStream_t side[2];
     cudaEvent_t fork;
     cudaEvent_t join[2];
+    // the triangle-record pass runs on its own stream, beside the whole
+    // grid build (it needs only the vertices), joined before the build ends
+    cudaStream_t rec;
+    cudaEvent_t rec_fork;
+    cudaEvent_t rec_join;
 };
 void launch_build(const BuildArgs& a, cudaStream_t st, const BuildFork* fork = nullptr);
 
 // Build kernels by work shape (grid sizing per task).
-enum BuildKind { BK_BBOX = 0, BK_ZERO, BK_TRI, BK_TILE, BK_SSMALL, BK_SMED, BK_SLARGE, BK_REFS, kBuildKinds };
+enum BuildKind { BK_BBOX = 0, BK_ZERO, BK_TRI, BK_TILE, BK_SSMALL, BK_SMED, BK_SLARGE, BK_REFS, BK_RECS, kBuildKinds };
 // Per-task block counts of every build kernel (the single-scene grid sizes).
 void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]);
 // Batch launch: total[k] blocks for kernel kind k, first[k] a device prefix
