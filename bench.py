@@ -341,7 +341,7 @@ def run_gpu(args, rank, ws, local, dist):
             best, allres, source = {x: fixed[x] for x in fixed if x != "k"}, [], "fixed"
         else:
             best, allres = tune_k(k)
-            source = "search"
+            source = autotune.search.last_source
         tuned[k] = dict(best=best, all=[(c, round(m, 4)) for c, m in allres], source=source)
         _save_autotune(f"deforming_k{k}", allres)
         order = best["order"]
@@ -946,7 +946,7 @@ def run_skewed(args, rank, ws, local, dist):
     else:
         space = {"k": LAMBDAS, "order": ("scanline", "morton8"), "empty_run": (2, 4, 8), "persistent": (True,),
                  "heavy_cell": (0, 24, 48), "heavy_lanes": (16, 32), "cell_records": (False, True),
-                 "refill": (0, 16)}
+                 "refill": (0, 16), "block": (128, 64, 256)}
         best, allres = autotune.search(measure, space=space, reps=2)
         _save_autotune("skewed", allres)
     _apply_tuning(s, best)
@@ -1330,14 +1330,15 @@ def _parse_tuning(text):
     return {"k": int(d.get("k", 8)), "order": d.get("order", "morton8"), "empty_run": int(d.get("empty_run", 4)),
             "persistent": yes(d.get("persistent", "0")), "heavy_cell": int(d.get("heavy_cell", 0)),
             "heavy_lanes": int(d.get("heavy_lanes", 32)), "cell_records": yes(d.get("cell_records", "0")),
-            "refill": int(d.get("refill", 0))}
+            "refill": int(d.get("refill", 0)), "block": int(d.get("block", 128))}
 
 
 def _apply_tuning(scene, cfg):
     """Launch-shape settings of one candidate; cell records take effect at the next build."""
     scene.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"],
                      heavy_cell=cfg.get("heavy_cell", 0), heavy_lanes=cfg.get("heavy_lanes", 32),
-                     cell_records=cfg.get("cell_records", False), refill=cfg.get("refill", 0))
+                     cell_records=cfg.get("cell_records", False), refill=cfg.get("refill", 0),
+                     block=cfg.get("block", 128))
 
 
 def _tune_str(cfg) -> str:
@@ -1347,7 +1348,7 @@ def _tune_str(cfg) -> str:
         return ""
     return (f"{cfg.get('order', '')}/er{cfg.get('empty_run', '')}/p{int(bool(cfg.get('persistent', 0)))}"
             f"/h{cfg.get('heavy_cell', 0)}x{cfg.get('heavy_lanes', 32)}/r{cfg.get('refill', 0)}"
-            f"/c{int(bool(cfg.get('cell_records', 0)))}")
+            f"/c{int(bool(cfg.get('cell_records', 0)))}/b{cfg.get('block', 128)}")
 
 
 def _r(x, n=3):

@@ -1201,6 +1201,11 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
             if (value < 0 || value > 32) return fail(RTG_INVALID_PARAM, "refill threshold must be 0..32");
             s->tune.refill = value;
             return RTG_OK;
+        case RTG_TUNE_BLOCK:
+            if (value != 64 && value != 128 && value != 256)
+                return fail(RTG_INVALID_PARAM, "trace block size must be 64, 128 or 256");
+            s->tune.block = value;
+            return RTG_OK;
         default:
             return fail(RTG_INVALID_PARAM, "unknown tuning key");
     }

@@ -106,6 +106,7 @@ struct TraceTuning {
     int heavy_lanes = 32;  // lanes per deferred ray in that pass: 4, 8, 16 or 32
     int refill = -1;       // > 0: idle lanes take new rays once this many are idle (0: finish each batch of 32);
                            // -1 (default): 16 for rays given as arrays, off for camera and frame traces
+    int block = 128;       // threads per block of the one-lane trace launch: 64, 128 or 256
 };
 // The refill threshold of a launch over camera-generated rays (camera and
 // frame traces: coherent, and in a frame each lane's shadow ray follows its

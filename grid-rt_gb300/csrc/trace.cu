@@ -325,7 +325,10 @@ __global__ void __launch_bounds__(128) trace_instances_kernel(const InstanceRec*
                 if (active && advance<MODE, ER>(P, L, offs, ids, tris, R->view.wald, occ, crec, kNoHeavy, kNoHeavy, cells, tests)) {
                     active = false;
                     if (L.id >= 0) {
-                        gbest = L.best;
+                        // the next instance compares against the exact
+                        // distance (the walk may have accepted its hit on
+                        // Moller-Trumbore's t)
+                        gbest = wald_f_of(L, L.id, R->view.wald);
                         gid = L.id;
                         ginst = i;
                         if (MODE == MODE_ANY) alive = false;   // occluded

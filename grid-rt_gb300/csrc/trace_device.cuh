@@ -278,6 +278,70 @@ __device__ __forceinline__ bool test_tri(Lane& L, int32_t tid, const float4& A, 
 #endif
 }
 
+// hitWald's f alone (the exact distance of a hit that test_tri_fast accepted
+// without the reference's test, when a later decision compares against it).
+__device__ __forceinline__ float wald_f_of(const Lane& L, int32_t tid, const float4* __restrict__ wald) {
+    const float4 a0 = __ldg(wald + 3 * (int64_t)tid);
+    const uint32_t k = __float_as_uint(a0.x);
+    const uint32_t ku = k == 2 ? 0 : k + 1, kv = k == 0 ? 2 : k - 1;
+    const float dk = pick3(L.dx, L.dy, L.dz, k), du = pick3(L.dx, L.dy, L.dz, ku), dv = pick3(L.dx, L.dy, L.dz, kv);
+    const float ok = pick3(L.ox, L.oy, L.oz, k), ou = pick3(L.ox, L.oy, L.oz, ku), ov = pick3(L.ox, L.oy, L.oz, kv);
+    const float nd = frcp(fadd(fadd(dk, fmul(a0.y, du)), fmul(a0.z, dv)));
+    return fmul(nd, fsub(fsub(fsub(a0.w, ok), fmul(a0.y, ou)), fmul(a0.z, ov)));
+}
+
+// The one-lane walk's test (the same decisions as test_tri).  A candidate
+// that Moller-Trumbore puts clearly inside the triangle -- every barycentric
+// at least kMtBarySlack inside, t at least the t slack inside the window,
+// below the best so far and (any-hit) away from tmax -- is one the
+// reference's test accepts too (both tests' errors stay far inside those
+// margins), so it is accepted at once with Moller-Trumbore's t as the best
+// so far (`fast_best`); only the candidates near an edge or a bound go to the
+// reference's test, after the best so far has been replaced by its exact
+// value.  The walk ends at the first cell with a hit, so a fast best never
+// outlives its cell's list, and the reported values are recomputed exactly
+// from the winner's record.
+template <int MODE>
+__device__ __forceinline__ bool test_tri_fast(Lane& L, int32_t tid, const float4& A, const float4& B,
+                                              const float4& C, float hi, const float4* __restrict__ wald,
+                                              bool& fast_best) {
+#if GRIDRT_DECIDE_WALD
+    const float tvx = L.ox - A.x, tvy = L.oy - A.y, tvz = L.oz - A.z;
+    const float px = L.dy * C.z - L.dz * C.y;
+    const float py = L.dz * C.x - L.dx * C.z;
+    const float pz = L.dx * C.y - L.dy * C.x;
+    const float det = B.x * px + B.y * py + B.z * pz;
+    float idet;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(idet) : "f"(det));
+    const float u = (tvx * px + tvy * py + tvz * pz) * idet;
+    if (!(u >= -kMtBarySlack)) return false;
+    const float qx = tvy * B.z - tvz * B.y;
+    const float qy = tvz * B.x - tvx * B.z;
+    const float qz = tvx * B.y - tvy * B.x;
+    const float v = (L.dx * qx + L.dy * qy + L.dz * qz) * idet;
+    const float w = (1.0f - u) - v;
+    if (!(v >= -kMtBarySlack && w >= -kMtBarySlack)) return false;
+    const float t = (C.x * qx + C.y * qy + C.z * qz) * idet;
+    const float ts = fabsf(t) * kMtTRelSlack + kHitEpsilon;
+    if (!((t < L.best + ts) && (t >= L.lo - ts) && (t <= hi + ts))) return false;
+    const bool any_phase = MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax);
+    if (u >= kMtBarySlack && v >= kMtBarySlack && w >= kMtBarySlack && t >= L.lo + ts && t <= hi - ts &&
+        t < L.best - ts && (!any_phase || t < L.tmax - ts || t > L.tmax + ts)) {
+        L.best = t;
+        L.id = tid;
+        fast_best = true;
+        return any_phase && t < L.tmax;
+    }
+    if (fast_best) {
+        L.best = wald_f_of(L, L.id, wald);
+        fast_best = false;
+    }
+    return wald_decide<MODE>(L, tid, hi, wald);
+#else
+    return test_tri<MODE>(L, tid, A, B, C, hi, wald);
+#endif
+}
+
 // Visits up to ER empty cells and at most one non-empty cell.
 // Returns true when the ray is finished (hit decided, or left the grid).
 template <int MODE, int ER>
@@ -308,6 +372,7 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
             L.work += e - b;
             const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
             tests += (uint32_t)(e - b);
+            bool fast_best = false;
             int32_t i = b;
             if (crec) {
                 // records stored in cell-list order: no id indirection
@@ -316,13 +381,13 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
                                  C0 = __ldg(crec + 3 * (int64_t)i + 2);
                     const float4 A1 = __ldg(crec + 3 * (int64_t)i + 3), B1 = __ldg(crec + 3 * (int64_t)i + 4),
                                  C1 = __ldg(crec + 3 * (int64_t)i + 5);
-                    if (test_tri<MODE>(L, __float_as_int(A0.w), A0, B0, C0, hi, wald)) return true;
-                    if (test_tri<MODE>(L, __float_as_int(A1.w), A1, B1, C1, hi, wald)) return true;
+                    if (test_tri_fast<MODE>(L, __float_as_int(A0.w), A0, B0, C0, hi, wald, fast_best)) return true;
+                    if (test_tri_fast<MODE>(L, __float_as_int(A1.w), A1, B1, C1, hi, wald, fast_best)) return true;
                 }
                 if (i < e) {
                     const float4 A0 = __ldg(crec + 3 * (int64_t)i), B0 = __ldg(crec + 3 * (int64_t)i + 1),
                                  C0 = __ldg(crec + 3 * (int64_t)i + 2);
-                    if (test_tri<MODE>(L, __float_as_int(A0.w), A0, B0, C0, hi, wald)) return true;
+                    if (test_tri_fast<MODE>(L, __float_as_int(A0.w), A0, B0, C0, hi, wald, fast_best)) return true;
                 }
                 i = e;
             }
@@ -332,14 +397,14 @@ __device__ __forceinline__ bool advance(const SParams& P, Lane& L, const int32_t
                              C0 = __ldg(tris + 3 * (int64_t)t0 + 2);
                 const float4 A1 = __ldg(tris + 3 * (int64_t)t1), B1 = __ldg(tris + 3 * (int64_t)t1 + 1),
                              C1 = __ldg(tris + 3 * (int64_t)t1 + 2);
-                if (test_tri<MODE>(L, t0, A0, B0, C0, hi, wald)) return true;
-                if (test_tri<MODE>(L, t1, A1, B1, C1, hi, wald)) return true;
+                if (test_tri_fast<MODE>(L, t0, A0, B0, C0, hi, wald, fast_best)) return true;
+                if (test_tri_fast<MODE>(L, t1, A1, B1, C1, hi, wald, fast_best)) return true;
             }
             if (i < e) {
                 const int32_t t0 = __ldg(ids + i);
                 const float4 A0 = __ldg(tris + 3 * (int64_t)t0), B0 = __ldg(tris + 3 * (int64_t)t0 + 1),
                              C0 = __ldg(tris + 3 * (int64_t)t0 + 2);
-                if (test_tri<MODE>(L, t0, A0, B0, C0, hi, wald)) return true;
+                if (test_tri_fast<MODE>(L, t0, A0, B0, C0, hi, wald, fast_best)) return true;
             }
             if (L.id >= 0) {
                 // a hit closer than the best on entry (the one-geometry walk
@@ -715,8 +780,8 @@ __device__ __forceinline__ void trace_refill(const SParams& P, const SceneView& 
     }
 }
 
-template <int MODE, bool COUNT, int ER>
-__global__ void __launch_bounds__(128, GRIDRT_TRACE_MIN_BLOCKS) trace_kernel(SceneView s, TraceIO io) {
+template <int MODE, bool COUNT, int ER, int TPB>
+__global__ void __launch_bounds__(TPB, GRIDRT_TRACE_MIN_BLOCKS * 128 / TPB) trace_kernel(SceneView s, TraceIO io) {
     pdl_begin();
     __shared__ SParams P;
     load_sparams(s.params, P);
@@ -1084,22 +1149,30 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
     }
 }
 
-// Blocks of 128 threads.  Persistent: as many blocks as fit on the device at
-// once, warps loop over ray batches.  One-shot: one batch per warp, blocks
-// scheduled by the hardware.
-template <int MODE, bool COUNT, int ER>
-inline void launch_er(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+// Blocks of TPB threads (the RTG_TUNE_BLOCK choice; counter launches use
+// 128).  Persistent: as many blocks as fit on the device at once, warps loop
+// over ray batches.  One-shot: one batch per warp, blocks scheduled by the
+// hardware.
+template <int MODE, bool COUNT, int ER, int TPB>
+inline void launch_tpb(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_kernel<MODE, COUNT, ER>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_kernel<MODE, COUNT, ER, TPB>, TPB, 0);
         per_sm = b > 0 ? b : 1;
     }
-    long long blocks = (io.n + 127) / 128;
+    long long blocks = (io.n + TPB - 1) / TPB;
     if (tune.persistent) blocks = blocks < (long long)per_sm * num_sms ? blocks : (long long)per_sm * num_sms;
     if (blocks < 1) blocks = 1;
     if (blocks > 0x7fffffffLL) blocks = 0x7fffffffLL;
-    launch_k(trace_kernel<MODE, COUNT, ER>, (unsigned)blocks, 128, 0, st, s, io);
+    launch_k(trace_kernel<MODE, COUNT, ER, TPB>, (unsigned)blocks, TPB, 0, st, s, io);
+}
+
+template <int MODE, bool COUNT, int ER>
+inline void launch_er(const SceneView& s, const TraceIO& io, const TraceTuning& tune, int num_sms, cudaStream_t st) {
+    if (COUNT || tune.block == 128) launch_tpb<MODE, COUNT, ER, 128>(s, io, tune, num_sms, st);
+    else if (tune.block == 64) launch_tpb<MODE, COUNT, ER, COUNT ? 128 : 64>(s, io, tune, num_sms, st);
+    else launch_tpb<MODE, COUNT, ER, COUNT ? 128 : 256>(s, io, tune, num_sms, st);
 }
 
 template <int MODE, bool COUNT>

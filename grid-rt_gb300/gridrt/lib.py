@@ -25,6 +25,7 @@ RTG_TRACE_COUNTERS = 1
 RTG_TUNE_EMPTY_RUN = 1
 RTG_TUNE_PERSISTENT = 2
 RTG_TUNE_CELL_RECORDS = 3
+RTG_TUNE_BLOCK = 7
 RTG_TUNE_HEAVY_CELL = 4
 RTG_TUNE_HEAVY_LANES = 5
 RTG_TUNE_REFILL = 6
@@ -437,7 +438,9 @@ class Scene:
         check(load().rtg_trace_frame_wait(self.h, int(ticket)))
 
     def set_tuning(self, empty_run: int = None, persistent: bool = None, cell_records: bool = None,
-                   heavy_cell: int = None, heavy_lanes: int = None, refill: int = None):
+                   heavy_cell: int = None, heavy_lanes: int = None, refill: int = None, block: int = None):
+        if block is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_BLOCK, int(block)))
         if empty_run is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:

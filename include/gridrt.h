@@ -480,14 +480,17 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *                        incoherent rays: +50 to +65% on random in-box rays at 16; 8 gains a
  *                        little more there and costs ~5% on camera rays); 0 off.  Unset, it is
  *                        16 for rays given as arrays (nearest, any, batches) and off for camera
- *                        and frame traces, whose lanes follow a camera ray with its shadow ray */
+ *                        and frame traces, whose lanes follow a camera ray with its shadow ray
+ *   RTG_TUNE_BLOCK       threads per block of the one-lane trace launch: 64, 128 (default) or 256
+ *                        (every block size keeps 64 registers a thread and 32 warps an SM) */
 enum {
     RTG_TUNE_EMPTY_RUN = 1,
     RTG_TUNE_PERSISTENT = 2,
     RTG_TUNE_CELL_RECORDS = 3,
     RTG_TUNE_HEAVY_CELL = 4,
     RTG_TUNE_HEAVY_LANES = 5,
-    RTG_TUNE_REFILL = 6
+    RTG_TUNE_REFILL = 6,
+    RTG_TUNE_BLOCK = 7
 };
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 

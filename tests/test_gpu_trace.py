@@ -137,17 +137,18 @@ def test_counters_match_oracle(gridlib, oracle):
 
 def test_results_independent_of_launch_tuning(gridlib, oracle):
     """Launch shape (empty-cell run, persistent vs one-shot grid, lane refill
-    threshold) never changes a result bit."""
+    threshold, threads per block) never changes a result bit."""
     import torch
     sc = scenes.deforming_sphere(3)
     s = _scene(gridlib, sc, 4)
     cam = scenes.deforming_sphere_camera(256, 256)
     n = cam.width * cam.height
     ref = None
-    for er, persistent, refill in [(e, p, 0) for e in (2, 4, 8, 16) for p in (True, False)] + \
-            [(e, p, r) for e in (2, 8) for p in (True, False) for r in (1, 16, 32)]:
+    for er, persistent, refill, block in [(e, p, 0, 128) for e in (2, 4, 8, 16) for p in (True, False)] + \
+            [(e, p, r, 128) for e in (2, 8) for p in (True, False) for r in (1, 16, 32)] + \
+            [(4, p, r, b) for p in (True, False) for r in (0, 16) for b in (64, 256)]:
         if True:
-            s.set_tuning(empty_run=er, persistent=persistent, refill=refill)
+            s.set_tuning(empty_run=er, persistent=persistent, refill=refill, block=block)
             d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
             d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
             d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
@@ -158,7 +159,7 @@ def test_results_independent_of_launch_tuning(gridlib, oracle):
                 ref = out
             else:
                 for a, b in zip(ref, out):
-                    assert np.array_equal(a, b), (er, persistent, refill)
+                    assert np.array_equal(a, b), (er, persistent, refill, block)
 
 
 def _frame(s, cam, order="morton8"):
