@@ -298,6 +298,28 @@ def run_gpu(args, rank, ws, local, dist):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
 
+    fixed = _parse_tuning(args.fixed_tuning)
+    if args.profile_frames:
+        # profiling run: the fixed tuning's k, a capacity build, then
+        # `profile_frames` frames launched call by call (deform, build, frame
+        # trace) -- no tuning search, graphs, end-to-end leg or CPU legs, so
+        # a profiler's capture ends quickly
+        k = fixed["k"] if fixed else HEADLINE_K
+        if fixed:
+            _apply_tuning(s, fixed)
+        s.deform(d_base, d_nrm, 0.05, 3.0, 0.0)
+        s.build(k)
+        order = fixed["order"] if fixed else "morton8"
+        with torch.cuda.stream(stream):
+            for f in range(args.profile_frames):
+                s.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+                s.build_async(k)
+                s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order)
+        torch.cuda.synchronize()
+        if s.build_check() != 0:
+            raise RuntimeError("profiled build failed: " + lib.load().rtg_last_error().decode())
+        return None
+
     # capacities for every frame at every k (synchronous builds, untimed)
     for k in LAMBDAS:
         for f in range(FRAMES):
@@ -333,7 +355,6 @@ def run_gpu(args, rank, ws, local, dist):
         return autotune.search(measure, reps=3)
 
     tuned = {}
-    fixed = _parse_tuning(args.fixed_tuning)
     per_k = {}
     sampler = ClockSampler(local).start() if rank == 0 else None
     for k in ([fixed["k"]] if fixed else LAMBDAS):
@@ -1252,7 +1273,8 @@ def run_serving(args, rank, ws, local, dist):
         # (in_flight 1); plain_pipelined keeps three such requests in flight
         if in_flight is None:
             in_flight = 1 if plain else 3
-        admit, done = lib.serve(scs, reqs, pool_bytes=pool_bytes, plain=plain, max_in_flight=in_flight)
+        admit, done = lib.serve(scs, reqs, pool_bytes=pool_bytes, plain=plain, max_in_flight=in_flight,
+                                max_step_rays=args.serve_step_rays)
         arr = np.array([q[0] for q in reqs])
         lat = done - arr
         rays = sum(q[4] for q in reqs)
@@ -1312,6 +1334,7 @@ def run_serving(args, rank, ws, local, dist):
                    "scene_bytes": int(scene_bytes), "pool_bytes": pool_bytes, "hbm_budget_bytes": budget,
                    "rays_per_request": "log-uniform [1e3, 4e6]", "modes": "70% closest / 30% any-hit",
                    "max_in_flight": {"served": 3, "plain": 1, "plain_pipelined": 3},
+                   "max_step_rays": args.serve_step_rays,
                    "refill": args.serve_refill},
         "saturation": saturation, "served_over_plain": round(saturation["served"]["mrays_s"] /
                                                               saturation["plain"]["mrays_s"], 3),
@@ -1443,11 +1466,17 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
     ap.add_argument("--serve-rates", default="10,100,1000,2000")
+    ap.add_argument("--serve-step-rays", type=int, default=0,
+                    help="rays a serving step admits at most (a larger request still forms a step alone); "
+                         "0: the library's default")
     ap.add_argument("--serve-refill", type=int, default=8,
                     help="lane-refill threshold of the serving scenes (served and plain paths alike)")
     ap.add_argument("--fixed-tuning", default="",
                     help="skip the autotuner: e.g. k=8,order=morton8,empty_run=4,persistent=0 (profiling runs)")
     ap.add_argument("--detail", default="", help="also write every workload's full result to this JSON file")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="profiling runs: only this many deforming-sphere frames (build + frame trace), "
+                         "launched call by call with --fixed-tuning's k and shape; prints nothing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, ws, local, dist = _dist()
@@ -1463,7 +1492,7 @@ def main():
         full = run_gpu(args, rank, ws, local, dist)
         detail["deforming"] = full
         subs = {}
-        if args.workload == "default" and ws == 1:
+        if args.workload == "default" and ws == 1 and not args.profile_frames:
             import argparse as _ap
             import torch
             serve_args = _ap.Namespace(**vars(args))

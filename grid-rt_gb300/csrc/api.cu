@@ -320,6 +320,7 @@ rtg_status rtg_scene_create(int device, void* stream, rtg_scene* out) {
         ok = ok && cudaEventCreateWithFlags(&s->fork.join[1], cudaEventDisableTiming) == cudaSuccess;
         ok = ok && cudaStreamCreateWithFlags(&s->fork.rec, cudaStreamNonBlocking) == cudaSuccess;
         ok = ok && cudaEventCreateWithFlags(&s->fork.rec_fork, cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&s->fork.rec_clear, cudaEventDisableTiming) == cudaSuccess;
         ok = ok && cudaEventCreateWithFlags(&s->fork.rec_join, cudaEventDisableTiming) == cudaSuccess;
         s->have_fork = ok;
         if (!ok) cudaGetLastError();
@@ -380,6 +381,7 @@ rtg_status rtg_scene_destroy(rtg_scene s) {
         cudaStreamDestroy(s->fork.rec);
     }
     if (s->fork.rec_fork) cudaEventDestroy(s->fork.rec_fork);
+    if (s->fork.rec_clear) cudaEventDestroy(s->fork.rec_clear);
     if (s->fork.rec_join) cudaEventDestroy(s->fork.rec_join);
     cudaFree(s->d_fring);
     for (int i = 0; i < 2; ++i) {

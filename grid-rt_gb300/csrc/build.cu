@@ -143,11 +143,17 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
     const float V = fmul(fmul(diag[0], diag[1]), diag[2]);
     const int32_t kn = (int32_t)((uint32_t)k * (uint32_t)ntris);
     const float q = fdiv(__int2float_rn(kn), V);
-    // powf(q, 1/3): the device evaluates pow in double and rounds to float;
-    // the host's powf may differ from that by one ulp, so the resolution is
-    // accepted only when ceil(d*f) is the same for f-1ulp, f, f+1ulp.
-    const float f = __double2float_rn(pow((double)q, (double)(1.0f / 3.0f)));
-    const float fm = nextafterf(f, 0.0f), fp = nextafterf(f, INFINITY);
+    // powf(q, 1/3): the reference's C library powf is within one ulp of the
+    // correctly rounded value and the device's single-precision powf within
+    // a few ulps of it (CUDA's documented bound), so the resolution is
+    // accepted only when ceil(d*f') is the same at both ends of a 16-ulp band
+    // around the device's f (ceil(d*f') is monotonic in f'); otherwise the
+    // host recomputes the parameters with the C library's powf.  (Evaluating
+    // pow in double here made the last block's serial parameter step several
+    // microseconds long: FP64 is a slow path on this GPU.)
+    const float f = powf(q, 1.0f / 3.0f);
+    const float fm = (f > 0.0f && isfinite(f)) ? __uint_as_float(__float_as_uint(f) - 16u) : f;
+    const float fp = (f > 0.0f && isfinite(f)) ? __uint_as_float(__float_as_uint(f) + 16u) : f;
     uint32_t status = 0;
     int64_t ncells = 1;
     for (int d = 0; d < 3; ++d) {
@@ -179,21 +185,31 @@ __device__ __forceinline__ void bbox_params_body(const float* __restrict__ verts
     if (status) atomicOr(&w->sticky, status);
 }
 
+// clear = 0: a clear kernel on the record stream clears the offsets and the
+// bitmap (a single-scene build with side streams), and this pass only
+// reduces the box.
 template <bool MULTI>
 __global__ void __launch_bounds__(256) bbox_params_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
-                       int ntasks) {
+                       int ntasks, int clear) {
     pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
         const BuildArgs& a = many[t];
         const unsigned vbx = blockIdx.x - (unsigned)first[t], vgx = (unsigned)(first[t + 1] - first[t]);
-        zero_capacity(a.offsets, a.occ, a.cell_cap, vbx, vgx);
+        if (clear) zero_capacity(a.offsets, a.occ, a.cell_cap, vbx, vgx);
         bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, vbx, vgx);
     } else {
         const BuildArgs& a = one;
-        zero_capacity(a.offsets, a.occ, a.cell_cap, blockIdx.x, gridDim.x);
+        if (clear) zero_capacity(a.offsets, a.occ, a.cell_cap, blockIdx.x, gridDim.x);
         bbox_params_body(a.verts, a.nverts, a.work, a.params, a.k, a.ntris, a.cell_cap, blockIdx.x, gridDim.x);
     }
+}
+
+// The offsets capacity and the bitmap cleared on the record stream, beside
+// the box pass (nothing in it depends on the grid parameters).
+__global__ void __launch_bounds__(256) clear_kernel(BuildArgs one) {
+    pdl_begin();
+    zero_capacity(one.offsets, one.occ, one.cell_cap, blockIdx.x, gridDim.x);
 }
 
 static __device__ __forceinline__ bool fatal(uint32_t s) {
@@ -1124,9 +1140,19 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     // frame's traces, which read the records -- and the build's end waits
     // for it), else first on `st`
     const bool rec_side = fork && fork->rec;
+    const bool side_clear = rec_side && !MULTI && !skip_bbox;
+    int bbox_blocks = g.total[BK_BBOX];
     if (rec_side) {
         cudaEventRecord(fork->rec_fork, st);
         cudaStreamWaitEvent(fork->rec, fork->rec_fork, 0);
+        if (side_clear) {
+            count_launches(1);
+            launch_k(clear_kernel, g.total[BK_BBOX], 256, 0, fork->rec, one);
+            cudaEventRecord(fork->rec_clear, fork->rec);
+            // the box pass alone: four vertices a thread at least
+            bbox_blocks = (int)((one.nverts + 1023) / 1024);
+            bbox_blocks = bbox_blocks < 1 ? 1 : (bbox_blocks > 2 * one.num_sms ? 2 * one.num_sms : bbox_blocks);
+        }
     }
     launch_k(records_kernel<MULTI>, g.total[BK_RECS], 256, 0, rec_side ? fork->rec : st, one, many, f[BK_RECS],
              ntasks);
@@ -1134,9 +1160,11 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     // the box pass also clears the offsets and the bitmap; host-resolved
     // parameters skip it and clear them on their own
     if (!skip_bbox)
-        launch_k(bbox_params_kernel<MULTI>, g.total[BK_BBOX], 256, 0, st, one, many, f[BK_BBOX], ntasks);
+        launch_k(bbox_params_kernel<MULTI>, bbox_blocks, 256, 0, st, one, many, f[BK_BBOX], ntasks,
+                 side_clear ? 0 : 1);
     else
         launch_k(zero_offsets_kernel<MULTI>, g.total[BK_ZERO], 256, 0, st, one, many, f[BK_ZERO], ntasks);
+    if (side_clear) cudaStreamWaitEvent(st, fork->rec_clear, 0);
     launch_k(count_kernel<MULTI>, g.total[BK_TRI], 256, 0, st, one, many, f[BK_TRI], ntasks);
     launch_k(scan_reduce_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);
     launch_k(scan_down_kernel<MULTI>, g.total[BK_TILE], SCAN_THREADS, 0, st, one, many, f[BK_TILE], ntasks);

@@ -53,6 +53,7 @@ struct BuildFork {
     // grid build (it needs only the vertices), joined before the build ends
     cudaStream_t rec;
     cudaEvent_t rec_fork;
+    cudaEvent_t rec_clear;   // the offsets and bitmap cleared (the count pass waits for it)
     cudaEvent_t rec_join;
 };
 void launch_build(const BuildArgs& a, cudaStream_t st, const BuildFork* fork = nullptr);
@@ -140,7 +141,8 @@ inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
 // need distinct slots.
 struct TraceSlot {
     unsigned long long* ctr;   // 8 words: ray claims, deferred rays, deferred claims, huge rays, huge claims,
-                               // huge entries at the queue's back (lists of kHugeLong+), at its front
+                               // huge entries at the queue's back (lists of kHugeLong+), at its front,
+                               // claims of front entries by the cluster pass's blocks
     int2* defer;          // {ray, cell} entries
     int32_t defer_cap;
     int2* huge = nullptr; // {ray, cell} entries of rays at a list above kHugeList (nullptr: no block pass)

@@ -126,10 +126,12 @@ def _check_against_regular(gridlib, L, verts, idx, k):
 
 
 def _resolution_is_ambiguous(verts, ntris, k):
-    """The device's test, restated in float32: the grid box enlarged by 1%
-    (Aabb::scaleBy), V, k * N / V, f = pow(q, 1/3) rounded from double, and
-    whether ceil(extent * f) changes between f - 1 ulp and f + 1 ulp on some
-    axis (then the host's powf decides the resolution)."""
+    """Whether the resolution rule sits on a powf ulp boundary, in float32:
+    the grid box enlarged by 1% (Aabb::scaleBy), V, k * N / V, f = pow(q, 1/3)
+    rounded from double, and whether ceil(extent * f) changes between
+    f - 1 ulp and f + 1 ulp on some axis.  The device flags a build whenever
+    ceil changes across a wider band around its own powf (then the host's
+    powf decides the resolution), so such a scene always takes that path."""
     f32 = np.float32
     mn, mx = verts.min(0).astype(f32), verts.max(0).astype(f32)
     s = np.where(mn == mx, f32(0.01), (np.abs(mx - mn) * f32(0.01)).astype(f32)).astype(f32)
