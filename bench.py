@@ -1466,9 +1466,9 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--serve-saturation", type=int, default=2000)
     ap.add_argument("--serve-rates", default="10,100,1000,2000")
-    ap.add_argument("--serve-step-rays", type=int, default=0,
+    ap.add_argument("--serve-step-rays", type=int, default=1 << 22,
                     help="rays a serving step admits at most (a larger request still forms a step alone); "
-                         "0: the library's default")
+                         "0: the library's default (16 M)")
     ap.add_argument("--serve-refill", type=int, default=8,
                     help="lane-refill threshold of the serving scenes (served and plain paths alike)")
     ap.add_argument("--fixed-tuning", default="",

@@ -141,8 +141,7 @@ inline void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sme
 // need distinct slots.
 struct TraceSlot {
     unsigned long long* ctr;   // 8 words: ray claims, deferred rays, deferred claims, huge rays, huge claims,
-                               // huge entries at the queue's back (lists of kHugeLong+), at its front,
-                               // claims of front entries by the cluster pass's blocks
+                               // huge entries at the queue's back (lists of kHugeLong+), at its front
     int2* defer;          // {ray, cell} entries
     int32_t defer_cap;
     int2* huge = nullptr; // {ray, cell} entries of rays at a list above kHugeList (nullptr: no block pass)

@@ -28,8 +28,6 @@
 // those that then meet a dense cluster's list in a block-per-ray pass.
 #pragma once
 
-#include <cooperative_groups.h>
-
 #include "common.cuh"
 #include "kernels.h"
 
@@ -1105,178 +1103,39 @@ __device__ __forceinline__ void block_walk(const SParams& P, const SceneView& s,
     }
 }
 
-// Cluster variant of the block-per-ray pass.  The rays queued at the back of
-// the huge-list queue met a list of kHugeLong+ entries (the dense cluster's
-// cells, up to ~70,000 entries): a thread-block cluster of kHugeCluster
-// blocks walks each of them together -- every list split over all the
-// cluster's threads, each block reducing its share, the blocks' (t, id) pairs
-// exchanged through distributed shared memory at a cluster barrier, every
-// block taking the same minimum (t, then smaller id = earlier entry) -- so
-// the longest rays finish kHugeCluster times sooner instead of running on
-// alone at the end of the pass.  When no such ray is left, each block of the
-// cluster claims the front of the queue on its own, as the block pass does.
-// Every block of a cluster holds the same ray state and takes the same
-// branches, so all of them meet every cluster barrier.
-static constexpr int kHugeCluster = 8;
-
-// List entry j's Moller-Trumbore record and triangle id: from the
-// cell-ordered records when the scene keeps them, else through the id list.
-__device__ __forceinline__ void load_entry(int32_t j, const int32_t* __restrict__ ids,
-                                           const float4* __restrict__ tris, const float4* __restrict__ crec,
-                                           float4& A, float4& B, float4& C, int32_t& t) {
-    if (crec) {
-        A = __ldg(crec + 3 * (int64_t)j);
-        B = __ldg(crec + 3 * (int64_t)j + 1);
-        C = __ldg(crec + 3 * (int64_t)j + 2);
-        t = __float_as_int(A.w);
-    } else {
-        t = __ldg(ids + j);
-        A = __ldg(tris + 3 * (int64_t)t);
-        B = __ldg(tris + 3 * (int64_t)t + 1);
-        C = __ldg(tris + 3 * (int64_t)t + 2);
-    }
-}
-
-__device__ __forceinline__ void cluster_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
-                                             uint32_t& cells, uint32_t& tests, float* red_t, int32_t* red_id,
-                                             float* cl_t, int32_t* cl_id) {
-    namespace cg = cooperative_groups;
-    cg::cluster_group cluster = cg::this_cluster();
-    const unsigned rank = cluster.block_rank();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
-    const int32_t stride = kHugeCluster * kHugeThreads;
-    const bool counter = rank == 0 && threadIdx.x == 0;
-    while (!done) {
-        if (counter) ++cells;
-        const int32_t w = (L.x >> 2) + (L.y >> 2) * P.bx + (L.z >> 1) * P.bxby;
-        if (__ldg(s.occ + w) & occ_bit(L.x, L.y, L.z)) {
-            const int32_t c = L.x + L.y * nx + L.z * nxy;
-            const int32_t b = __ldg(s.offsets + c), e = __ldg(s.offsets + c + 1);
-            const float hi = fadd(vmin(vmin(L.tMx, L.tMy), L.tMz), kHitEpsilon);
-            if (counter) tests += (uint32_t)(e - b);
-            Lane T = L;
-            T.id = -1;
-            for (int32_t i = b + (int32_t)(rank * kHugeThreads + threadIdx.x); i < e; i += stride) {
-                float4 A, B, C;
-                int32_t t;
-                load_entry(i, s.ids, s.tris, s.crec, A, B, C, t);
-                test_tri<MODE_NEAREST>(T, t, A, B, C, hi, s.wald);
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ot = __shfl_xor_sync(FULL, T.best, o);
-                const int32_t oid = __shfl_xor_sync(FULL, T.id, o);
-                if (ot < T.best || (ot == T.best && (uint32_t)oid < (uint32_t)T.id)) {
-                    T.best = ot;
-                    T.id = oid;
-                }
-            }
-            if (lane == 0) {
-                red_t[wid] = T.best;
-                red_id[wid] = T.id;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                float bt = red_t[0];
-                int32_t bid = red_id[0];
-                for (int i = 1; i < kHugeThreads / 32; ++i)
-                    if (red_t[i] < bt || (red_t[i] == bt && (uint32_t)red_id[i] < (uint32_t)bid)) {
-                        bt = red_t[i];
-                        bid = red_id[i];
-                    }
-                *cl_t = bt;
-                *cl_id = bid;
-            }
-            cluster.sync();
-            float bt = kFltMax;
-            int32_t bid = -1;
-            for (unsigned r = 0; r < (unsigned)kHugeCluster; ++r) {
-                const float rt = *cluster.map_shared_rank(cl_t, r);
-                const int32_t rid = *cluster.map_shared_rank(cl_id, r);
-                if (rid >= 0 && (bid < 0 || rt < bt || (rt == bt && (uint32_t)rid < (uint32_t)bid))) {
-                    bt = rt;
-                    bid = rid;
-                }
-            }
-            cluster.sync();   // every block has read the others' pairs before they change
-            if (bid >= 0) {
-                // the first cell with a hit ends the walk; any-hit:
-                // occluded only below tmax
-                L.best = bt;
-                L.id = (any && !(bt < L.tmax)) ? -1 : bid;
-                done = true;
-                continue;
-            }
-        }
-        if (dda_step(P, L)) {
-            L.id = -1;
-            done = true;
-        }
-    }
-}
-
 template <int MODE, bool COUNT>
-__global__ void __cluster_dims__(kHugeCluster, 1, 1) __launch_bounds__(kHugeThreads)
-    trace_huge_cluster_kernel(SceneView s, TraceIO io) {
-    namespace cg = cooperative_groups;
+__global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, TraceIO io) {
     pdl_begin();
-    cg::cluster_group cluster = cg::this_cluster();
     __shared__ SParams P;
     __shared__ float red_t[kHugeThreads / 32];
     __shared__ int32_t red_id[kHugeThreads / 32];
-    __shared__ float cl_t;
-    __shared__ int32_t cl_id;
     __shared__ unsigned long long claim;
     load_sparams(s.params, P);
     unsigned long long nh = io.counter[3];
     if (nh > (unsigned long long)io.huge_cap) nh = (unsigned long long)io.huge_cap;
-    unsigned long long nb = io.counter[5];   // entries at the queue's back: lists of kHugeLong+
-    if (nb > nh) nb = nh;
-    const unsigned long long nf = nh - nb;   // entries at its front
+    // the rays at the longest lists (the queue's back) are claimed first, so
+    // they do not start last and run on alone at the end of the pass
+    const unsigned long long nb = io.counter[5];
     uint32_t cells = 0, tests = 0;
-    // the back of the queue, one ray per cluster
     for (;;) {
-        if (cluster.block_rank() == 0 && threadIdx.x == 0) claim = atomicAdd(io.counter + 4, 1ull);
-        cluster.sync();
-        const unsigned long long j = *cluster.map_shared_rank(&claim, 0);
-        cluster.sync();
-        if (j >= nb) break;
-        const int2 d = __ldg(io.huge + ((unsigned long long)io.huge_cap - 1 - j));
-        const bool shadow = MODE == MODE_FRAME && d.x < 0;   // MODE_FRAME: a shadow ray (in its slot)
-        Lane L;
-        L.ray = shadow ? -1 - d.x : d.x;
-        bool done = shadow ? !start_ray<MODE_ANY>(P, io, L, L.ray) : !start_ray<MODE>(P, io, L, L.ray);
-        if (done) {
-            if (L.id != -2) L.id = -1;
-        } else {
-            resume_at(P, L, d.y);
-        }
-        const bool writer = cluster.block_rank() == 0 && threadIdx.x == 0;
-        for (int phase = 0; phase < 2; ++phase) {
-            cluster_walk(P, s, L, done, MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax), cells,
-                         tests, red_t, red_id, &cl_t, &cl_id);
-            if (!finish_ray<MODE>(io, P, s, L, writer)) break;
-            done = false;
-        }
-    }
-    // the front of the queue, one ray per block
-    for (;;) {
-        if (threadIdx.x == 0) claim = atomicAdd(io.counter + 7, 1ull);
+        if (threadIdx.x == 0) claim = atomicAdd(io.counter + 4, 1ull);
         __syncthreads();
         const unsigned long long j = claim;
         __syncthreads();
-        if (j >= nf) break;
-        const int2 d = __ldg(io.huge + j);
-        const bool shadow = MODE == MODE_FRAME && d.x < 0;
+        if (j >= nh) break;
+        const int2 d = __ldg(io.huge + (j < nb ? (unsigned long long)io.huge_cap - 1 - j : j - nb));
+        const bool shadow = MODE == MODE_FRAME && d.x < 0;   // MODE_FRAME: a shadow ray (in its slot)
         Lane L;
         L.ray = shadow ? -1 - d.x : d.x;
+        // the same on every thread
         bool done = shadow ? !start_ray<MODE_ANY>(P, io, L, L.ray) : !start_ray<MODE>(P, io, L, L.ray);
         if (done) {
             if (L.id != -2) L.id = -1;
         } else {
             resume_at(P, L, d.y);
         }
+        // one walk, or for a MODE_FRAME camera ray two: its own, then from
+        // its start the shadow ray every thread sets up from the hit
         for (int phase = 0; phase < 2; ++phase) {
             block_walk(P, s, L, done, MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax), cells, tests,
                        red_t, red_id);
@@ -1350,24 +1209,13 @@ inline void launch_wide(const SceneView& s, const TraceIO& io, const TraceTuning
 // can hold.
 template <int MODE, bool COUNT>
 inline void launch_huge(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
-    // as many clusters as can be resident at once
-    static int clusters = 0;
-    if (clusters == 0) {
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_huge_cluster_kernel<MODE, COUNT>, kHugeThreads,
-                                                      0);
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)(kHugeCluster * num_sms));
-        cfg.blockDim = dim3(kHugeThreads);
-        int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, trace_huge_cluster_kernel<MODE, COUNT>, &cfg) != cudaSuccess || n < 1) {
-            cudaGetLastError();
-            n = per_sm > 0 ? per_sm * num_sms / kHugeCluster : 1;
-        }
-        clusters = n > 0 ? n : 1;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_huge_kernel<MODE, COUNT>, kHugeThreads, 0);
+        per_sm = b > 0 ? b : 1;
     }
-    launch_k(trace_huge_cluster_kernel<MODE, COUNT>, (unsigned)(clusters * kHugeCluster), kHugeThreads, 0, st, s,
-             io);
+    launch_k(trace_huge_kernel<MODE, COUNT>, (unsigned)(per_sm * num_sms), kHugeThreads, 0, st, s, io);
 }
 
 template <int MODE>
@@ -1382,7 +1230,7 @@ inline void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.huge = defer ? slot.huge : nullptr;
     io.huge_cap = io.huge ? slot.huge_cap : 0;
     count_launches(defer ? (io.huge ? 3 : 2) : 1);
-    cudaMemsetAsync(slot.ctr, 0, 8 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(slot.ctr, 0, 7 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {

@@ -227,11 +227,12 @@ def test_heavy_cell_counters_match_oracle(gridlib, oracle):
 @pytest.mark.parametrize("ntris", [1 << 16, 1 << 18])
 def test_huge_list_block_pass_is_exact(gridlib, oracle, ntris):
     """Lists above 2,048 entries (59,000 / 236,000 triangles in a 0.1^3
-    cluster, k = 4) go from the group pass to the block-per-ray pass -- lists
-    of 16,384+ entries (the larger scene) to its thread-block-cluster phase:
-    hit words, frame outputs, occlusion and traversal counters equal the
-    one-lane walk's (with the records read through the id lists and in cell
-    order), and the hits meet the oracle's near-tie rules."""
+    cluster, k = 4) go from the group pass to the block-per-ray pass -- rays
+    at lists of 16,384+ entries (the larger scene) from the back of its
+    queue, claimed first: hit words, frame outputs, occlusion and traversal
+    counters equal the one-lane walk's (with the records read through the id
+    lists and in cell order), and the hits meet the oracle's near-tie
+    rules."""
     sc = scenes.skewed_density(n=ntris)
     s = _scene(gridlib, sc, 4)      # a synchronous build: the scene knows its longest list
     g = oracle.Grid(sc.verts, sc.idx, 4)
