@@ -1358,10 +1358,11 @@ def _parse_tuning(text):
 
 def _apply_tuning(scene, cfg):
     """Launch-shape settings of one candidate; cell records take effect at the next build."""
+    block = cfg.get("block", 128)
     scene.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"],
                      heavy_cell=cfg.get("heavy_cell", 0), heavy_lanes=cfg.get("heavy_lanes", 32),
                      cell_records=cfg.get("cell_records", False), refill=cfg.get("refill", 0),
-                     block=cfg.get("block", 128))
+                     block=None if block == 128 else block)
 
 
 def _tune_str(cfg) -> str:
