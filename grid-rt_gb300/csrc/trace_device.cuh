@@ -1024,12 +1024,80 @@ __global__ void __launch_bounds__(128, GRIDRT_WIDE_MIN_BLOCKS) trace_wide_kernel
 #define GRIDRT_HUGE_THREADS 256
 #endif
 static constexpr int kHugeThreads = GRIDRT_HUGE_THREADS;
+#ifndef GRIDRT_HUGE_MIN_BLOCKS
+#define GRIDRT_HUGE_MIN_BLOCKS 3
+#endif
 static_assert(kHugeThreads % 32 == 0 && kHugeThreads <= 1024, "block-per-ray pass: whole warps, one block");
+
+// Crowded lists staged in shared memory.  With cell-ordered records a list
+// is one contiguous run of 48-byte records, so the bulk-copy engine
+// (cp.async.bulk, completion counted on an mbarrier per buffer) copies it
+// into a ring of kStageDepth shared-memory buffers of kStageEntries records:
+// while the block tests one chunk the next kStageDepth - 1 are in flight,
+// and no thread waits on its own global loads.  A chunk costs a block
+// barrier and a wait, so chunks are large: 768 records (36 KB), two
+// buffers, 72 KB a block and three blocks an SM (smaller chunks or deeper
+// rings measured slower).  Lists shorter than kStageMin keep the direct
+// loads.  Every wait is bounded: a copy that has
+// not landed after kStageWaitLimit polls sets bit 0 of the launch's counter
+// word 7, the chunk is tested from global memory and the block stops
+// staging.
+#ifndef GRIDRT_STAGE
+#define GRIDRT_STAGE 1
+#endif
+#ifndef GRIDRT_STAGE_ENTRIES
+#define GRIDRT_STAGE_ENTRIES 768
+#endif
+#ifndef GRIDRT_STAGE_DEPTH
+#define GRIDRT_STAGE_DEPTH 2
+#endif
+static constexpr int kStageEntries = GRIDRT_STAGE_ENTRIES;
+static constexpr int kStageDepth = GRIDRT_STAGE_DEPTH;
+static constexpr size_t kStageBytes = GRIDRT_STAGE ? (size_t)kStageDepth * 3 * kStageEntries * sizeof(float4) : 0;
+static_assert(kStageDepth >= 2 && kStageDepth <= 16, "stage ring depth");
+static constexpr int32_t kStageMin = 2 * kHugeThreads;
+static constexpr uint32_t kStageWaitLimit = 1u << 24;
+static_assert(kStageEntries % kHugeThreads == 0 || kHugeThreads % kStageEntries == 0, "stage chunk");
+
+struct Stage {
+    float4* buf;          // shared: kStageDepth x kStageEntries x 3 float4
+    uint64_t* bar;        // shared: one mbarrier per buffer
+    int* off;             // shared: 1 once a wait has run out
+    uint32_t phase;       // bit q: the parity of buffer q's next completion
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Thread 0: buffer `dst` <- `bytes` of global memory at `src`, completion
+// on `bar` (which expects those bytes and thread 0's arrival).
+__device__ __forceinline__ void stage_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait for the completion of `bar`'s phase of parity `parity`.
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kStageWaitLimit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
 
 // The block's ray (identical state on every thread) walked to its end:
 // each list split over the block, a block reduction per list.
 __device__ __forceinline__ void block_walk(const SParams& P, const SceneView& s, Lane& L, bool done, bool any,
-                                           uint32_t& cells, uint32_t& tests, float* red_t, int32_t* red_id) {
+                                           uint32_t& cells, uint32_t& tests, float* red_t, int32_t* red_id,
+                                           Stage* st = nullptr, unsigned long long* err = nullptr) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int32_t nx = P.res[0], nxy = P.res[0] * P.res[1];
     while (!done) {
@@ -1042,9 +1110,64 @@ __device__ __forceinline__ void block_walk(const SParams& P, const SceneView& s,
             if (threadIdx.x == 0) tests += (uint32_t)(e - b);
             Lane T = L;
             T.id = -1;
-            // two entries a thread per step, both loaded before either is
-            // tested (the same entries in the same order as one a step)
-            if (s.crec) {
+            if (GRIDRT_STAGE && st && s.crec && e - b >= kStageMin && !*st->off) {
+                // staged: chunk ch in buffer ch % kStageDepth, the next
+                // kStageDepth - 1 chunks in flight
+                const int32_t nch = (e - b + kStageEntries - 1) / kStageEntries;
+                if (threadIdx.x == 0) {
+                    for (int32_t ch = 0; ch < nch && ch < kStageDepth; ++ch) {
+                        const int32_t cb = b + ch * kStageEntries;
+                        const int32_t cn = e - cb < kStageEntries ? e - cb : kStageEntries;
+                        stage_copy(st->buf + ch * 3 * kStageEntries, s.crec + 3 * (int64_t)cb, (uint32_t)cn * 48u,
+                                   st->bar + ch);
+                    }
+                }
+                for (int32_t ch = 0; ch < nch; ++ch) {
+                    const int q = ch % kStageDepth;
+                    const int32_t cb = b + ch * kStageEntries;
+                    const int32_t cn = e - cb < kStageEntries ? e - cb : kStageEntries;
+                    const bool ok = stage_wait(st->bar + q, (st->phase >> q) & 1u);
+                    st->phase ^= 1u << q;
+                    if (ok) {
+                        const float4* sb = st->buf + q * 3 * kStageEntries;
+                        for (int32_t j = (int32_t)threadIdx.x; j < cn; j += kHugeThreads) {
+                            const float4 A = sb[3 * j], B = sb[3 * j + 1], C = sb[3 * j + 2];
+                            test_tri<MODE_NEAREST>(T, __float_as_int(A.w), A, B, C, hi, s.wald);
+                        }
+                    }
+                    // every thread is done with buffer q before chunk
+                    // ch + kStageDepth is copied into it
+                    if (__syncthreads_or(!ok)) {
+                        // a copy has not landed: wait once more (bounded) for
+                        // it and the copies in flight behind it, test the rest
+                        // of the list from global memory, stop staging
+                        if (!ok) stage_wait(st->bar + q, ((st->phase >> q) & 1u) ^ 1u);
+                        for (int32_t k = ch + 1; k < nch && k < ch + kStageDepth; ++k) {
+                            const int qk = k % kStageDepth;
+                            stage_wait(st->bar + qk, (st->phase >> qk) & 1u);
+                        }
+                        if (threadIdx.x == 0) {
+                            *st->off = 1;
+                            if (err) atomicOr(err, 1ull);
+                        }
+                        for (int32_t i = (ok ? cb + cn : cb) + (int32_t)threadIdx.x; i < e; i += kHugeThreads) {
+                            const float4 A = __ldg(s.crec + 3 * (int64_t)i), B = __ldg(s.crec + 3 * (int64_t)i + 1),
+                                         C = __ldg(s.crec + 3 * (int64_t)i + 2);
+                            test_tri<MODE_NEAREST>(T, __float_as_int(A.w), A, B, C, hi, s.wald);
+                        }
+                        __syncthreads();
+                        break;
+                    }
+                    if (threadIdx.x == 0 && ch + kStageDepth < nch) {
+                        const int32_t nb = cb + kStageDepth * kStageEntries;
+                        const int32_t nn = e - nb < kStageEntries ? e - nb : kStageEntries;
+                        stage_copy(st->buf + q * 3 * kStageEntries, s.crec + 3 * (int64_t)nb, (uint32_t)nn * 48u,
+                                   st->bar + q);
+                    }
+                }
+            } else if (s.crec) {
+                // two entries a thread per step, both loaded before either is
+                // tested (the same entries in the same order as one a step)
                 for (int32_t i = b + (int32_t)threadIdx.x; i < e; i += 2 * kHugeThreads) {
                     const int32_t i2 = i + kHugeThreads;
                     const float4 A = __ldg(s.crec + 3 * (int64_t)i), B = __ldg(s.crec + 3 * (int64_t)i + 1),
@@ -1110,12 +1233,22 @@ __device__ __forceinline__ void block_walk(const SParams& P, const SceneView& s,
 }
 
 template <int MODE, bool COUNT>
-__global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, TraceIO io) {
+__global__ void __launch_bounds__(kHugeThreads, GRIDRT_HUGE_MIN_BLOCKS) trace_huge_kernel(SceneView s, TraceIO io) {
     pdl_begin();
     __shared__ SParams P;
     __shared__ float red_t[kHugeThreads / 32];
     __shared__ int32_t red_id[kHugeThreads / 32];
     __shared__ unsigned long long claim;
+    extern __shared__ __align__(128) float4 stage_buf[];   // kStageBytes (dynamic)
+    __shared__ __align__(8) uint64_t stage_bar[kStageDepth];
+    __shared__ int stage_off;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < kStageDepth; ++q)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(stage_bar + q)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stage_off = 0;
+    }
+    Stage stage{stage_buf, stage_bar, &stage_off, 0u};
     load_sparams(s.params, P);
     unsigned long long nh = io.counter[3];
     if (nh > (unsigned long long)io.huge_cap) nh = (unsigned long long)io.huge_cap;
@@ -1144,7 +1277,7 @@ __global__ void __launch_bounds__(kHugeThreads) trace_huge_kernel(SceneView s, T
         // its start the shadow ray every thread sets up from the hit
         for (int phase = 0; phase < 2; ++phase) {
             block_walk(P, s, L, done, MODE == MODE_ANY || (MODE == MODE_FRAME && L.tmax > -kFltMax), cells, tests,
-                       red_t, red_id);
+                       red_t, red_id, &stage, io.counter + 7);
             if (!finish_ray<MODE>(io, P, s, L, threadIdx.x == 0)) break;
             done = false;
         }
@@ -1217,11 +1350,15 @@ template <int MODE, bool COUNT>
 inline void launch_huge(const SceneView& s, const TraceIO& io, int num_sms, cudaStream_t st) {
     static int per_sm = 0;
     if (per_sm == 0) {
+        // the staging ring is dynamic shared memory (above the 48 KB of a
+        // static allocation for deep rings)
+        cudaFuncSetAttribute(trace_huge_kernel<MODE, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kStageBytes);
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_huge_kernel<MODE, COUNT>, kHugeThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, trace_huge_kernel<MODE, COUNT>, kHugeThreads, kStageBytes);
         per_sm = b > 0 ? b : 1;
     }
-    launch_k(trace_huge_kernel<MODE, COUNT>, (unsigned)(per_sm * num_sms), kHugeThreads, 0, st, s, io);
+    launch_k(trace_huge_kernel<MODE, COUNT>, (unsigned)(per_sm * num_sms), kHugeThreads, kStageBytes, st, s, io);
 }
 
 template <int MODE>
@@ -1236,7 +1373,7 @@ inline void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.huge = defer ? slot.huge : nullptr;
     io.huge_cap = io.huge ? slot.huge_cap : 0;
     count_launches(defer ? (io.huge ? 3 : 2) : 1);
-    cudaMemsetAsync(slot.ctr, 0, 7 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(slot.ctr, 0, 8 * sizeof(unsigned long long), st);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {

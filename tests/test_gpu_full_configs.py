@@ -59,12 +59,19 @@ def test_deforming_sphere_full_frame(gridlib, oracle, k):
                            sc.verts, sc.idx, oracle)
 
 
-def test_skewed_density_full(gridlib, oracle):
+# k = 8 with the library's default tuning; k = 2 with the tuning the skewed
+# bench step uses (cell-ordered records, lists above 48 entries deferred to
+# 16-lane groups, lane refill), where the cluster's 18 lists above 2,048
+# entries send ~1,500 camera rays through the shared-list and block passes
+@pytest.mark.parametrize("k,tuning", [(8, None), (2, dict(heavy_cell=48, heavy_lanes=16, cell_records=True,
+                                                            refill=16, order="morton8"))])
+def test_skewed_density_full(gridlib, oracle, k, tuning):
     import torch
-    k = 8
     sc = scenes.skewed_density()
     s = gridlib.Scene(0)
     s.set_geometry(sc.verts, sc.idx)
+    if tuning:
+        s.set_tuning(**{x: v for x, v in tuning.items() if x != "order"})
     s.build(k)
     g = oracle.Grid(sc.verts, sc.idx, k)
     off, ids = s.download()
@@ -80,14 +87,14 @@ def test_skewed_density_full(gridlib, oracle):
     rays = scenes.camera_rays(cam, "morton8")
     st = parity.compare_hits(gridlib.split_hits(d_hits.cpu().numpy()), g.trace_closest(rays), sc.verts, sc.idx,
                              rays, oracle)
-    _report("skewed 1024^2 primary", st)
+    _report(f"skewed 1024^2 primary k={k}", st)
     parity.assert_parity(st)
     sec = d_sec.cpu().numpy()
     has = sec[:, 7] > 0
     sec_rays = np.ascontiguousarray(sec[has])
     sh = gridlib.split_hits(d_hits2.cpu().numpy()[has])
     st = parity.compare_hits(sh, g.trace_closest(sec_rays), sc.verts, sc.idx, sec_rays, oracle)
-    _report("skewed diffuse secondary", st)
+    _report(f"skewed diffuse secondary k={k}", st)
     parity.assert_parity(st)
 
 
