@@ -29,6 +29,7 @@
 #include "kernels.h"
 
 #include <climits>
+#include <cooperative_groups.h>
 
 namespace gridrt {
 
@@ -896,11 +897,16 @@ __global__ void __launch_bounds__(512) sort_medium_kernel(BuildArgs one, const B
 // one shared-memory bit per id (per id chunk, from a scratch copy, when the
 // scene has more triangles than the bitmap has bits), then the set bits
 // written back in order.
+// Lists above kSplitRefs entries of a single-scene build whose ids fit one
+// bitmap span are sorted by sort_split_kernel, the rest by sort_large.
+static constexpr int32_t kSplitRefs = SORT_BLOCK_MAX;
+static constexpr int kSplitBlocks = 8;   // blocks of a list's cluster (the portable maximum)
+
 __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offsets,
                                                           int32_t* __restrict__ ids, int32_t* __restrict__ scratch,
                                                           const int32_t* __restrict__ q, const BuildWork* w,
                                                           const GridParams* p, int32_t bitmap_words, int64_t ntris,
-                                                          unsigned vbx, unsigned vgx) {
+                                                          unsigned vbx, unsigned vgx, bool skip_split = false) {
     if (sort_skip(p)) return;
     extern __shared__ uint32_t bm[];
     __shared__ int32_t sh_min[32], sh_max[32];
@@ -912,6 +918,7 @@ __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offs
     for (int64_t qi = vbx; qi < nq; qi += vgx) {
         const int32_t c = q[qi];
         const int32_t s = offsets[c], n = offsets[c + 1] - s;
+        if (skip_split && n > kSplitRefs) continue;
         if (n <= bitonic_max) {
             int32_t* a = reinterpret_cast<int32_t*>(bm);
             int m = 512;
@@ -1034,7 +1041,7 @@ __device__ __forceinline__ void sort_large_body(const int32_t* __restrict__ offs
 
 template <bool MULTI>
 __global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const BuildArgs* __restrict__ many, const int* __restrict__ first,
-                       int ntasks) {
+                       int ntasks, bool split) {
     pdl_begin();
     if (MULTI) {
         const int t = block_task(first, ntasks);
@@ -1042,7 +1049,104 @@ __global__ void __launch_bounds__(1024) sort_large_kernel(BuildArgs one, const B
         sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words, a.ntris, blockIdx.x - (unsigned)first[t], (unsigned)(first[t + 1] - first[t]));
     } else {
         const BuildArgs& a = one;
-        sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words, a.ntris, blockIdx.x, gridDim.x);
+        sort_large_body(a.offsets, a.ids, a.scratch, a.q_large, a.work, a.params, a.bitmap_words, a.ntris, blockIdx.x,
+                        gridDim.x, split);
+    }
+}
+
+// A list above kSplitRefs entries, split by triangle id over the
+// kSplitBlocks blocks of a thread-block cluster: block r owns the ids of
+// slice r of [0, ntris) and a shared-memory bitmap of that slice.  Each
+// block reads an eighth of the list and sets every entry's bit in the
+// owning block's bitmap through distributed shared memory; after a cluster
+// barrier each block counts its slice, reads the counts of the slices
+// before it from their blocks, and writes its slice's ids in order.  The
+// whole list has been read before the first barrier, so no entry is
+// overwritten before it is read.  One block per list had sorted the
+// longest list alone while the other SMs idled.
+__global__ void __launch_bounds__(1024) sort_split_kernel(BuildArgs a) {
+    pdl_begin();
+    if (sort_skip(a.params)) return;
+    extern __shared__ uint32_t sbm[];
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t slice_total;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int rank = (int)cl.block_rank();
+    const unsigned cid = blockIdx.x / kSplitBlocks, ncl = gridDim.x / kSplitBlocks;
+    const uint32_t nq = a.work->nsort[2];
+    const int64_t slice = ((a.ntris + kSplitBlocks - 1) / kSplitBlocks + 31) & ~(int64_t)31;
+    const int64_t lo = (int64_t)rank * slice;
+    const int64_t hi = lo + slice < a.ntris ? lo + slice : a.ntris;
+    const int words = hi > lo ? (int)((hi - lo + 31) >> 5) : 0;
+    uint32_t* peer_bm[kSplitBlocks];
+#pragma unroll
+    for (int r = 0; r < kSplitBlocks; ++r) peer_bm[r] = cl.map_shared_rank(sbm, r);
+    constexpr int kSortLoads = 4;
+    for (int64_t qi = cid; qi < nq; qi += ncl) {
+        const int32_t c = a.q_large[qi];
+        const int32_t s = a.offsets[c], n = a.offsets[c + 1] - s;
+        if (n <= kSplitRefs) continue;   // the same list on every block of the cluster
+        for (int i = threadIdx.x; i < words; i += blockDim.x) sbm[i] = 0u;
+        cl.sync();   // every bitmap cleared
+        // this block's eighth of the list
+        const int32_t part = (n + kSplitBlocks - 1) / kSplitBlocks;
+        const int32_t p0 = rank * part, p1 = p0 + part < n ? p0 + part : n;
+        for (int32_t t0 = p0 + (int32_t)threadIdx.x; t0 < p1; t0 += kSortLoads * (int32_t)blockDim.x) {
+            int32_t v[kSortLoads];
+#pragma unroll
+            for (int u = 0; u < kSortLoads; ++u) {
+                const int32_t t = t0 + u * (int32_t)blockDim.x;
+                v[u] = t < p1 ? a.ids[s + t] : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kSortLoads; ++u) {
+                if (t0 + u * (int32_t)blockDim.x < p1) {
+                    const int q = (int)((int64_t)v[u] / slice);
+                    const int64_t d = (int64_t)v[u] - (int64_t)q * slice;
+                    atomicOr(peer_bm[q] + (d >> 5), 1u << (d & 31));
+                }
+            }
+        }
+        cl.sync();   // every bit set, the whole list read
+        // each thread owns a contiguous run of this block's words
+        const int per = (words + blockDim.x - 1) / blockDim.x;
+        const int w0 = (int)threadIdx.x * per < words ? (int)threadIdx.x * per : words;
+        const int w1 = w0 + per < words ? w0 + per : words;
+        int cnt = 0;
+        for (int i = w0; i < w1; ++i) cnt += __popc(sbm[i]);
+        int x = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[wid] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int i = 0; i < nw; ++i) {
+                const int t = warp_tot[i];
+                warp_tot[i] = run;
+                run += t;
+            }
+            slice_total = run;
+        }
+        cl.sync();   // every slice's count published
+        int below = 0;
+        for (int r = 0; r < rank; ++r) below += *cl.map_shared_rank(&slice_total, r);
+        int pos = s + below + warp_tot[wid] + x - cnt;
+        for (int i = w0; i < w1; ++i) {
+            uint32_t bits = sbm[i];
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                a.ids[pos++] = (int32_t)(lo + (int64_t)i * 32 + b);
+            }
+        }
+        // no block clears its bitmap or republishes its count for the next
+        // list while another may still read them
+        cl.sync();
     }
 }
 
@@ -1129,6 +1233,32 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
     out[BK_RECS] = clampi((a.ntris + 255) / 256, 16 * sms);
 }
 
+// launch_k with a thread-block cluster of `cluster` blocks along x.
+template <typename... KArgs, typename... Args>
+static void launch_cluster_k(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                             unsigned cluster, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[2];
+    unsigned na = 0;
+    attr[na].id = cudaLaunchAttributeClusterDimension;
+    attr[na].val.clusterDim.x = cluster;
+    attr[na].val.clusterDim.y = 1;
+    attr[na].val.clusterDim.z = 1;
+    ++na;
+#if GRIDRT_PDL
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+#endif
+    cfg.attrs = attr;
+    cfg.numAttrs = na;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <bool MULTI>
 static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int ntasks, const BatchGrid& g,
                               bool skip_bbox, int bitmap_words, cudaStream_t st, const BuildFork* fork = nullptr) {
@@ -1181,8 +1311,18 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     }
     launch_k(sort_small_kernel<MULTI>, g.total[BK_SSMALL], 256, 0, st, one, many, f[BK_SSMALL], ntasks);
     launch_k(sort_medium_kernel<MULTI>, g.total[BK_SMED], 512, 0, sm, one, many, f[BK_SMED], ntasks);
+    // a single-scene build whose ids fit one bitmap span sorts its lists
+    // above kSplitRefs entries with a cluster each, first (the longest work)
+    const bool split = !MULTI && one.ntris > 0 && one.ntris <= (int64_t)bitmap_words * 32;
+    if (split) {
+        count_launches(1);
+        const int clusters = one.num_sms / kSplitBlocks > 0 ? one.num_sms / kSplitBlocks : 1;
+        const int64_t words = ((one.ntris + kSplitBlocks - 1) / kSplitBlocks + 31) / 32 + 1;
+        launch_cluster_k(sort_split_kernel, (unsigned)(clusters * kSplitBlocks), 1024u, (size_t)words * 4, sl,
+                         (unsigned)kSplitBlocks, one);
+    }
     launch_k(sort_large_kernel<MULTI>, g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, sl, one, many,
-             f[BK_SLARGE], ntasks);
+             f[BK_SLARGE], ntasks, split);
     if (fork) {
         cudaEventRecord(fork->join[0], sm);
         cudaEventRecord(fork->join[1], sl);
