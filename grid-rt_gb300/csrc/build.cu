@@ -1235,8 +1235,8 @@ void build_blocks(const BuildArgs& a, int sms, int out[kBuildKinds]) {
 
 // launch_k with a thread-block cluster of `cluster` blocks along x.
 template <typename... KArgs, typename... Args>
-static void launch_cluster_k(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
-                             unsigned cluster, Args... args) {
+static cudaError_t launch_cluster_k(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                                    cudaStream_t st, unsigned cluster, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
@@ -1256,7 +1256,7 @@ static void launch_cluster_k(void (*kernel)(KArgs...), unsigned grid, unsigned b
 #endif
     cfg.attrs = attr;
     cfg.numAttrs = na;
-    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 template <bool MULTI>
@@ -1313,13 +1313,18 @@ static void launch_build_impl(const BuildArgs& one, const BuildArgs* many, int n
     launch_k(sort_medium_kernel<MULTI>, g.total[BK_SMED], 512, 0, sm, one, many, f[BK_SMED], ntasks);
     // a single-scene build whose ids fit one bitmap span sorts its lists
     // above kSplitRefs entries with a cluster each, first (the longest work)
-    const bool split = !MULTI && one.ntris > 0 && one.ntris <= (int64_t)bitmap_words * 32;
+    bool split = !MULTI && one.ntris > 0 && one.ntris <= (int64_t)bitmap_words * 32;
     if (split) {
-        count_launches(1);
         const int clusters = one.num_sms / kSplitBlocks > 0 ? one.num_sms / kSplitBlocks : 1;
         const int64_t words = ((one.ntris + kSplitBlocks - 1) / kSplitBlocks + 31) / 32 + 1;
-        launch_cluster_k(sort_split_kernel, (unsigned)(clusters * kSplitBlocks), 1024u, (size_t)words * 4, sl,
-                         (unsigned)kSplitBlocks, one);
+        if (launch_cluster_k(sort_split_kernel, (unsigned)(clusters * kSplitBlocks), 1024u, (size_t)words * 4, sl,
+                             (unsigned)kSplitBlocks, one) == cudaSuccess) {
+            count_launches(1);
+        } else {
+            // the cluster launch was refused: the block sort takes every list
+            (void)cudaGetLastError();
+            split = false;
+        }
     }
     launch_k(sort_large_kernel<MULTI>, g.total[BK_SLARGE], 1024, (size_t)bitmap_words * 4, sl, one, many,
              f[BK_SLARGE], ntasks, split);
