@@ -574,11 +574,11 @@ def _traffic_from_profiles(kernel: str, k: int):
 
 
 def _save_autotune(name: str, results):
-    """The full candidate table of one search, written beside the run's
-    output (directory from GRIDRT_BENCH_OUT, default gpurun_out/ when it
-    exists) instead of into the result line."""
-    out_dir = os.environ.get("GRIDRT_BENCH_OUT") or os.path.join(REPO, "gpurun_out")
-    if not results or not os.path.isdir(out_dir):
+    """The full candidate table of one search, written as
+    autotune_<name>.json into the directory GRIDRT_BENCH_OUT names (when it
+    is set and exists) instead of into the result line."""
+    out_dir = os.environ.get("GRIDRT_BENCH_OUT")
+    if not results or not out_dir or not os.path.isdir(out_dir):
         return
     try:
         with open(os.path.join(out_dir, f"autotune_{name}.json"), "w") as f:
@@ -677,7 +677,7 @@ def run_plain_small(args, rank, ws, local, dist):
     d_occ = torch.empty(npix, dtype=torch.uint8, device=dev)
     d_sr = torch.empty((npix, 8), dtype=torch.float32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    order = "morton8"
+    order = ["morton8"]
 
     def step(ev=None):
         with torch.cuda.stream(stream):
@@ -686,10 +686,32 @@ def run_plain_small(args, rank, ws, local, dist):
             s.build_async(k)
             if ev:
                 ev[1].record(stream)
-            s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order)
+            s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order[0])
             if ev:
                 ev[2].record(stream)
 
+    # the autotuner's launch shape and ray order for this step (results do
+    # not depend on them), each candidate timed on one step after one untimed
+    from gridrt import autotune
+
+    def measure(cfg):
+        _apply_tuning(s, cfg)
+        order[0] = cfg["order"]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        step()
+        step(ev)
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[2])
+
+    fixed = _parse_tuning(args.fixed_tuning)
+    if fixed:
+        best, allres, source = {x: fixed[x] for x in fixed if x != "k"}, [], "fixed"
+    else:
+        best, allres = autotune.search(measure, reps=3)
+        source = autotune.search.last_source
+    _save_autotune("plain_small", allres)
+    _apply_tuning(s, best)
+    order[0] = best["order"]
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -743,6 +765,7 @@ def run_plain_small(args, rank, ws, local, dist):
     cpu_s = sum(b + t for b, t, _ in cpu) / len(cpu)
     cpu_rays = cpu[0][2]
     return {"workload": "plane_debris_65536tri_512x512_shadow", "k": k, "value": round(rays / g_ms / 1e3, 2),
+            "tuning": _tune_str(best), "tuned_by": source,
             "ms_per_step": round(g_ms, 4), "build_ms": round(build_ms, 4),
             "trace_ms": round(trace_ms, 4), "rays_per_step": rays, "steps": args.steps,
             "cpu": {"value": round(cpu_rays / cpu_s / 1e6, 3), "ms_per_step": round(1e3 * cpu_s, 3),
