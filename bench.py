@@ -990,7 +990,7 @@ def run_skewed(args, rank, ws, local, dist):
     else:
         space = {"k": LAMBDAS, "order": ("scanline", "morton8"), "empty_run": (2, 4, 8), "persistent": (True,),
                  "heavy_cell": (0, 24, 48), "heavy_lanes": (16, 32), "cell_records": (False, True),
-                 "refill": (0, 16), "block": (128, 64, 256)}
+                 "refill": (0, 16), "block": (128, 64, 256), "lanes": (1, 2)}
         best, allres = autotune.search(measure, space=space, reps=2)
         _save_autotune("skewed", allres)
     _apply_tuning(s, best)
@@ -1376,16 +1376,17 @@ def _parse_tuning(text):
     return {"k": int(d.get("k", 8)), "order": d.get("order", "morton8"), "empty_run": int(d.get("empty_run", 4)),
             "persistent": yes(d.get("persistent", "0")), "heavy_cell": int(d.get("heavy_cell", 0)),
             "heavy_lanes": int(d.get("heavy_lanes", 32)), "cell_records": yes(d.get("cell_records", "0")),
-            "refill": int(d.get("refill", 0)), "block": int(d.get("block", 128))}
+            "refill": int(d.get("refill", 0)), "block": int(d.get("block", 128)), "lanes": int(d.get("lanes", 1))}
 
 
 def _apply_tuning(scene, cfg):
     """Launch-shape settings of one candidate; cell records take effect at the next build."""
-    block = cfg.get("block", 128)
+    # every setting is applied, defaults included, so no candidate inherits
+    # the one before it
     scene.set_tuning(empty_run=cfg["empty_run"], persistent=cfg["persistent"],
                      heavy_cell=cfg.get("heavy_cell", 0), heavy_lanes=cfg.get("heavy_lanes", 32),
                      cell_records=cfg.get("cell_records", False), refill=cfg.get("refill", 0),
-                     block=None if block == 128 else block)
+                     block=cfg.get("block", 128), lanes=cfg.get("lanes", 1))
 
 
 def _tune_str(cfg) -> str:
@@ -1395,7 +1396,7 @@ def _tune_str(cfg) -> str:
         return ""
     return (f"{cfg.get('order', '')}/er{cfg.get('empty_run', '')}/p{int(bool(cfg.get('persistent', 0)))}"
             f"/h{cfg.get('heavy_cell', 0)}x{cfg.get('heavy_lanes', 32)}/r{cfg.get('refill', 0)}"
-            f"/c{int(bool(cfg.get('cell_records', 0)))}/b{cfg.get('block', 128)}")
+            f"/c{int(bool(cfg.get('cell_records', 0)))}/b{cfg.get('block', 128)}/l{cfg.get('lanes', 1)}")
 
 
 def _r(x, n=3):

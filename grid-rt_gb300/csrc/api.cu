@@ -1208,6 +1208,11 @@ rtg_status rtg_scene_set_tuning(rtg_scene s, int32_t key, int32_t value) {
                 return fail(RTG_INVALID_PARAM, "trace block size must be 64, 128 or 256");
             s->tune.block = value;
             return RTG_OK;
+        case RTG_TUNE_LANES:
+            if (value != 1 && value != 2 && value != 4)
+                return fail(RTG_INVALID_PARAM, "lanes per ray must be 1, 2 or 4");
+            s->tune.lanes = value;
+            return RTG_OK;
         default:
             return fail(RTG_INVALID_PARAM, "unknown tuning key");
     }

@@ -108,6 +108,7 @@ struct TraceTuning {
     int refill = -1;       // > 0: idle lanes take new rays once this many are idle (0: finish each batch of 32);
                            // -1 (default): 16 for rays given as arrays, off for camera and frame traces
     int block = 128;       // threads per block of the one-lane trace launch: 64, 128 or 256
+    int lanes = 1;         // lanes per ray from the start: 1 (one-lane walk), 2 or 4 (group walk for every ray)
 };
 // The refill threshold of a launch over camera-generated rays (camera and
 // frame traces: coherent, and in a frame each lane's shadow ray follows its

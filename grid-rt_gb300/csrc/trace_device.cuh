@@ -965,8 +965,9 @@ __global__ void __launch_bounds__(128, GRIDRT_WIDE_MIN_BLOCKS) trace_wide_kernel
     __shared__ SParams P;
     load_sparams(s.params, P);
     const int lane = threadIdx.x & 31, gl = lane & (G - 1), grp = lane / G;
-    unsigned long long nd = io.counter[1];
-    if (nd > (unsigned long long)io.defer_cap) nd = (unsigned long long)io.defer_cap;
+    // the deferred rays, or (no queue: the group walk from the start) every ray
+    unsigned long long nd = io.defer ? io.counter[1] : (unsigned long long)io.n;
+    if (io.defer && nd > (unsigned long long)io.defer_cap) nd = (unsigned long long)io.defer_cap;
     uint32_t cells = 0, tests = 0;
     for (;;) {
         unsigned long long j0 = 0;
@@ -981,13 +982,13 @@ __global__ void __launch_bounds__(128, GRIDRT_WIDE_MIN_BLOCKS) trace_wide_kernel
         L.id = -1;
         bool shadow = false;      // MODE_FRAME: the entry is a shadow ray (its slot holds it)
         if (valid) {
-            const int2 d = __ldg(io.defer + j);
+            const int2 d = io.defer ? __ldg(io.defer + j) : make_int2((int32_t)j, -1);
             shadow = MODE == MODE_FRAME && d.x < 0;
             L.ray = shadow ? -1 - d.x : d.x;
             done = shadow ? !start_ray<MODE_ANY>(P, io, L, L.ray) : !start_ray<MODE>(P, io, L, L.ray);
             if (done) {
                 if (L.id != -2) L.id = -1;
-            } else {
+            } else if (d.y >= 0) {
                 resume_at(P, L, d.y);
             }
         }
@@ -1372,8 +1373,23 @@ inline void launch_mode(const SceneView& s, TraceIO io, const TraceSlot& slot, c
     io.refill = refill_for(tune, MODE == MODE_CAMERA || MODE == MODE_FRAME);
     io.huge = defer ? slot.huge : nullptr;
     io.huge_cap = io.huge ? slot.huge_cap : 0;
-    count_launches(defer ? (io.huge ? 3 : 2) : 1);
     cudaMemsetAsync(slot.ctr, 0, 8 * sizeof(unsigned long long), st);
+    if (tune.lanes > 1 && !io.ctr) {
+        // every ray walked by a group of lanes from its start (the group
+        // pass with no queue); lists above kHugeList are still handed to
+        // the block-per-ray pass
+        io.defer = nullptr;
+        io.defer_cap = 0;
+        io.heavy = kNoHeavy;
+        io.huge = slot.huge;
+        io.huge_cap = io.huge ? slot.huge_cap : 0;
+        count_launches(io.huge ? 2 : 1);
+        if (tune.lanes == 2) launch_wide_g<MODE, false, 2>(s, io, num_sms, st);
+        else launch_wide_g<MODE, false, 4>(s, io, num_sms, st);
+        if (io.huge) launch_huge<MODE, false>(s, io, num_sms, st);
+        return;
+    }
+    count_launches(defer ? (io.huge ? 3 : 2) : 1);
     if (io.ctr) launch_count<MODE, true>(s, io, tune, num_sms, st);
     else launch_count<MODE, false>(s, io, tune, num_sms, st);
     if (defer) {

@@ -2,7 +2,8 @@
 
 The space: cells per triangle k (when the caller lets it vary), ray tile
 order (scanline / Morton 8x8), empty-cell run length, persistent vs one-shot
-trace grid, threads per block of the one-lane trace launch, the list length
+trace grid, threads per block of the one-lane trace launch, lanes per ray
+from the start (one, or a group of 2 or 4 for every ray), the list length
 above which a ray is finished by the warp-per-ray pass and that pass's lanes
 per ray, cell-ordered triangle records, lane refill.  Each candidate is timed
 with a caller-supplied measurement (CUDA events on the scene's stream).
@@ -31,6 +32,7 @@ SPACE = {
     "empty_run": (4, 2, 8),
     "persistent": (True, False),
     "block": (128, 64, 256),
+    "lanes": (1, 2, 4),
     "heavy_cell": (32, 0, 24, 48),
     "heavy_lanes": (32, 16),
     "cell_records": (False, True),

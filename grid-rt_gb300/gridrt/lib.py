@@ -26,6 +26,7 @@ RTG_TUNE_EMPTY_RUN = 1
 RTG_TUNE_PERSISTENT = 2
 RTG_TUNE_CELL_RECORDS = 3
 RTG_TUNE_BLOCK = 7
+RTG_TUNE_LANES = 8
 RTG_TUNE_HEAVY_CELL = 4
 RTG_TUNE_HEAVY_LANES = 5
 RTG_TUNE_REFILL = 6
@@ -438,9 +439,12 @@ class Scene:
         check(load().rtg_trace_frame_wait(self.h, int(ticket)))
 
     def set_tuning(self, empty_run: int = None, persistent: bool = None, cell_records: bool = None,
-                   heavy_cell: int = None, heavy_lanes: int = None, refill: int = None, block: int = None):
+                   heavy_cell: int = None, heavy_lanes: int = None, refill: int = None, block: int = None,
+                   lanes: int = None):
         if block is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_BLOCK, int(block)))
+        if lanes is not None:
+            check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_LANES, int(lanes)))
         if empty_run is not None:
             check(load().rtg_scene_set_tuning(self.h, RTG_TUNE_EMPTY_RUN, int(empty_run)))
         if persistent is not None:

@@ -482,7 +482,13 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *                        16 for rays given as arrays (nearest, any, batches) and off for camera
  *                        and frame traces, whose lanes follow a camera ray with its shadow ray
  *   RTG_TUNE_BLOCK       threads per block of the one-lane trace launch: 64, 128 (default) or 256
- *                        (every block size keeps 64 registers a thread and 32 warps an SM) */
+ *                        (every block size keeps 64 registers a thread and 32 warps an SM)
+ *   RTG_TUNE_LANES       lanes that trace each ray from its start: 1 (default: one ray a lane,
+ *                        the long lists handed on as above), 2 or 4 (every ray walked by a group
+ *                        of lanes that splits each cell's list).  Groups pay on launches too
+ *                        small to fill the GPU with one ray a lane (65,536 triangles, 512^2
+ *                        camera rays + their shadow rays: +33% at 2) and cost on full ones
+ *                        (1024^2 frames: -44% at 2) */
 enum {
     RTG_TUNE_EMPTY_RUN = 1,
     RTG_TUNE_PERSISTENT = 2,
@@ -490,7 +496,8 @@ enum {
     RTG_TUNE_HEAVY_CELL = 4,
     RTG_TUNE_HEAVY_LANES = 5,
     RTG_TUNE_REFILL = 6,
-    RTG_TUNE_BLOCK = 7
+    RTG_TUNE_BLOCK = 7,
+    RTG_TUNE_LANES = 8
 };
 rtg_status rtg_scene_set_tuning(rtg_scene scene, int32_t key, int32_t value);
 

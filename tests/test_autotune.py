@@ -11,11 +11,11 @@ def _cost(cfg):
     # separable: each dimension has one best value
     return (abs(cfg["empty_run"] - 8) + (0 if cfg["order"] == "scanline" else 3) + abs(cfg["block"] - 64) / 64
             + (0 if cfg["persistent"] else 1) + abs(cfg["heavy_cell"] - 24) / 8 + (cfg["heavy_lanes"] != 16)
-            + (not cfg["cell_records"]) + cfg["refill"] / 16)
+            + (not cfg["cell_records"]) + cfg["refill"] / 16 + abs(cfg["lanes"] - 2))
 
 
 BEST = {"empty_run": 8, "order": "scanline", "block": 64, "persistent": True, "heavy_cell": 24,
-        "heavy_lanes": 16, "cell_records": True, "refill": 0}
+        "heavy_lanes": 16, "cell_records": True, "refill": 0, "lanes": 2}
 
 
 def test_descent_finds_separable_optimum():

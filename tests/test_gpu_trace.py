@@ -137,7 +137,7 @@ def test_counters_match_oracle(gridlib, oracle):
 
 def test_results_independent_of_launch_tuning(gridlib, oracle):
     """Launch shape (empty-cell run, persistent vs one-shot grid, lane refill
-    threshold, threads per block) never changes a result bit."""
+    threshold, threads per block, lanes per ray) never changes a result bit."""
     import torch
     sc = scenes.deforming_sphere(3)
     s = _scene(gridlib, sc, 4)
@@ -146,9 +146,12 @@ def test_results_independent_of_launch_tuning(gridlib, oracle):
     ref = None
     for er, persistent, refill, block in [(e, p, 0, 128) for e in (2, 4, 8, 16) for p in (True, False)] + \
             [(e, p, r, 128) for e in (2, 8) for p in (True, False) for r in (1, 16, 32)] + \
-            [(4, p, r, b) for p in (True, False) for r in (0, 16) for b in (64, 256)]:
+            [(4, p, r, b) for p in (True, False) for r in (0, 16) for b in (64, 256)] + \
+            [(4, True, 0, -2), (4, True, 0, -4)]:
         if True:
-            s.set_tuning(empty_run=er, persistent=persistent, refill=refill, block=block)
+            # block -2 / -4: every ray walked by a group of 2 / 4 lanes
+            lanes = -block if block < 0 else 1
+            s.set_tuning(empty_run=er, persistent=persistent, refill=refill, block=max(block, 64), lanes=lanes)
             d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
             d_sr = torch.empty((n, 8), dtype=torch.float32, device="cuda")
             d_occ = torch.empty(n, dtype=torch.uint8, device="cuda")
@@ -260,6 +263,15 @@ def test_huge_list_block_pass_is_exact(gridlib, oracle, ntris):
         assert np.array_equal(o0, s.trace_any(rays_any)), lanes
         for a, b in zip(f0, _frame(s, cam)):
             assert np.array_equal(a, b), lanes
+    # every ray walked by a group of lanes from its start, crowded lists
+    # still handed to the block-per-ray pass
+    for group in (2, 4):
+        s.set_tuning(lanes=group)
+        assert np.array_equal(h0.view(np.int32), s.trace_nearest(rays).view(np.int32)), group
+        assert np.array_equal(o0, s.trace_any(rays_any)), group
+        for a, b in zip(f0, _frame(s, cam)):
+            assert np.array_equal(a, b), group
+    s.set_tuning(lanes=1)
     st = parity.compare_hits(gridlib.split_hits(h0), g.trace_closest(rays), sc.verts, sc.idx, rays, oracle)
     _report("huge lists", st)
     parity.assert_parity(st)
