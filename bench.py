@@ -1213,6 +1213,22 @@ def run_render(args, rank, ws, local, dist):
     cam = scenes.plane_and_debris_camera(WIDTH, HEIGHT)
     d_rgb = torch.empty((WIDTH * HEIGHT, 3), dtype=torch.float32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    # lanes per ray for the bounce levels' trace launches (results do not
+    # depend on it), each candidate timed on one frame after one untimed
+    from gridrt import autotune
+
+    def measure(cfg):
+        s.set_tuning(lanes=cfg["lanes"])
+        s.render(cam, d_n, mats, lights, d_rgb, d_colors=d_c, d_material=d_m, max_depth=3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.render(cam, d_n, mats, lights, d_rgb, d_colors=d_c, d_material=d_m, max_depth=3)
+        return 1e3 * (time.perf_counter() - t0)
+
+    best, allres = autotune.search(measure, space={"lanes": (1, 2, 4)}, reps=3)
+    _save_autotune("render", allres)
+    s.set_tuning(lanes=best["lanes"])
     for _ in range(args.warmup):
         s.render(cam, d_n, mats, lights, d_rgb, d_colors=d_c, d_material=d_m, max_depth=3)
     torch.cuda.synchronize()
@@ -1234,6 +1250,7 @@ def run_render(args, rank, ws, local, dist):
         "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "render_plane_and_debris_1024x1024_depth3", "k": 4, "rays_per_step": rays // args.steps,
+                   "lanes": best["lanes"],
                    "timing": "host clock around the synchronous rtg_render call (per-level count read-backs "
                              "included); L2 flushed before each frame, outside the timed call"},
     })
