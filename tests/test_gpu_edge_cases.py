@@ -123,3 +123,22 @@ def test_one_triangle(gridlib, oracle):
     assert (gh["id"][inside] == 0).all()
     st = parity.compare_hits(gh, oh, v, idx, rays, oracle)
     parity.assert_parity(st)
+
+
+def test_tuning_values_checked(gridlib):
+    """Every launch-shape setting outside its documented values is refused
+    with RTG_INVALID_PARAM and leaves the scene's tuning as it was (a trace
+    after the refusals equals one before them)."""
+    sc = scenes.tiny_scene(3, 200)
+    s = gridlib.Scene(0)
+    s.set_geometry(sc.verts, sc.idx)
+    s.build(4)
+    rays = scenes.random_rays(np.random.default_rng(5), 4096, (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0))
+    before = s.trace_nearest(rays).view(np.int32).copy()
+    lib = gridlib.load()
+    bad = [(gridlib.RTG_TUNE_EMPTY_RUN, 3), (gridlib.RTG_TUNE_HEAVY_CELL, -1), (gridlib.RTG_TUNE_HEAVY_LANES, 5),
+           (gridlib.RTG_TUNE_REFILL, 33), (gridlib.RTG_TUNE_BLOCK, 100), (gridlib.RTG_TUNE_LANES, 3),
+           (gridlib.RTG_TUNE_LANES, 0), (99, 1)]
+    for key, value in bad:
+        assert lib.rtg_scene_set_tuning(s.h, key, value) == gridlib.RTG_INVALID_PARAM, (key, value)
+    assert np.array_equal(before, s.trace_nearest(rays).view(np.int32))
