@@ -397,13 +397,32 @@ __device__ __forceinline__ void count_body(const float* __restrict__ verts, cons
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)vbx * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)vgx * blockDim.x) >> 5;
+    // crowded cells: the block's additions gathered in a small
+    // direct-mapped shared table (a slot taken by the first cell that maps
+    // to it), flushed with one global atomic a slot at the end
+    constexpr int kHot = 32;
+    __shared__ int32_t hot_cell[kHot];
+    __shared__ int32_t hot_cnt[kHot];
+    if (threadIdx.x < kHot) {
+        hot_cell[threadIdx.x] = -1;
+        hot_cnt[threadIdx.x] = 0;
+    }
+    __syncthreads();
     for (int64_t base = warp * 32; base < ntris; base += nwarps * 32) {
         warp_expand(L, verts, idx, ntris, base, p, w, [&](int32_t cell, int32_t, bool active) {
             const unsigned peers = __match_any_sync(FULL, cell);
             const int leader = __ffs(peers) - 1;
-            if (active && lane == leader) atomicAdd(&counts[cell], __popc(peers));
+            if (active && lane == leader) {
+                const int slot = (int)(((uint32_t)cell * 2654435761u) >> 27);
+                const int32_t old = atomicCAS(&hot_cell[slot], -1, cell);
+                if (old == -1 || old == cell) atomicAdd(&hot_cnt[slot], __popc(peers));
+                else atomicAdd(&counts[cell], __popc(peers));
+            }
         });
     }
+    __syncthreads();
+    if (threadIdx.x < kHot && hot_cell[threadIdx.x] >= 0 && hot_cnt[threadIdx.x] > 0)
+        atomicAdd(&counts[hot_cell[threadIdx.x]], hot_cnt[threadIdx.x]);
 }
 
 template <bool MULTI>
