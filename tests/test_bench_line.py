@@ -1,0 +1,48 @@
+"""The bench's one result line (no GPU): built from a full result of the
+default run on a GB300 (tests/fixtures/bench_detail_gb300.json, written by
+`bench.py --detail`), it carries every key of the result-line contract, the
+roofline, CPU-baseline, end-to-end, launch-count and clock objects, one
+small object per further workload, and stays a few KB long."""
+import importlib.util
+import json
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _bench():
+    spec = importlib.util.spec_from_file_location("bench", os.path.join(HERE, "..", "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_default_line_contract():
+    bench = _bench()
+    with open(os.path.join(HERE, "fixtures", "bench_detail_gb300.json")) as f:
+        d = json.load(f)
+    subs = {"cfg0_plain": d["cfg0_plain"], "cfg2_skewed": bench.compact_skewed(d["cfg2_skewed"]),
+            "cfg3_batched": bench.compact_batched(d["cfg3_batched"]),
+            "cfg4_serving": bench.compact_serving(d["cfg4_serving"])}
+    line = bench.compact_line(d["deforming"], subs)
+    text = json.dumps(line, separators=(",", ":"))
+    assert len(text) < 4096, len(text)
+    back = json.loads(text)
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "roofline", "cpu_baseline", "e2e",
+                "gpu_launches", "clocks"):
+        assert key in back, key
+    assert back["value"] > 0 and back["n_gpus"] == 1 and back["higher_is_better"] is True
+    assert back["warmup"] >= 3 and back["scaling"] == "weak"
+    assert back["config"]["workload"] and "l2" in back["config"]
+    rf = back["roofline"]
+    assert rf["bound"] in ("hbm", "tensor") and 0 < rf["frac"] < 2 and rf["achieved"] > 0 and rf["peak"] > 0
+    assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-3
+    cb = back["cpu_baseline"]
+    assert cb["value"] > 0 and cb["cores"] >= 1 and cb["kind"] in ("port", "reference")
+    e = back["e2e"]
+    assert e["value"] > 0 and e["h2d_bytes_per_step"] > 0 and e["d2h_bytes_per_step"] > 0
+    assert isinstance(back["gpu_launches"], int) and back["gpu_launches"] > 0
+    assert back["clocks"]["sm_mhz"] > 0 and isinstance(back["clocks"]["reasons"], list)
+    for name in subs:
+        assert name in back and back[name].get("value", 0) > 0, name
