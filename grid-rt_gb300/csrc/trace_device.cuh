@@ -1039,10 +1039,9 @@ static_assert(kHugeThreads % 32 == 0 && kHugeThreads <= 1024, "block-per-ray pas
 // barrier and a wait, so chunks are large: 768 records (36 KB), two
 // buffers, 72 KB a block and three blocks an SM (smaller chunks or deeper
 // rings measured slower).  Lists shorter than kStageMin keep the direct
-// loads.  Every wait is bounded: a copy that has
-// not landed after kStageWaitLimit polls sets bit 0 of the launch's counter
-// word 7, the chunk is tested from global memory and the block stops
-// staging.
+// loads.  Every wait is bounded: a copy that has not landed after
+// kStageWaitLimit polls sets bit 0 of the launch's counter word 7, the rest
+// of the list is tested from global memory and the block stops staging.
 #ifndef GRIDRT_STAGE
 #define GRIDRT_STAGE 1
 #endif
