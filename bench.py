@@ -38,10 +38,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-
-# every kernel module loaded when the CUDA context is created, so no timed
-# region pays for loading one on its first launch
-os.environ.setdefault("CUDA_MODULE_LOADING", "EAGER")
 import statistics
 import subprocess
 import sys
