@@ -487,7 +487,7 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
  *                        the long lists handed on as above), 2 or 4 (every ray walked by a group
  *                        of lanes that splits each cell's list).  Groups pay on launches too
  *                        small to fill the GPU with one ray a lane (65,536 triangles, 512^2
- *                        camera rays + their shadow rays: +33% at 2) and cost on full ones
+ *                        camera rays + their shadow rays: +41% at 2) and cost on full ones
  *                        (1024^2 frames: -44% at 2) */
 enum {
     RTG_TUNE_EMPTY_RUN = 1,
