@@ -26,8 +26,11 @@ Default run (one JSON line, rank 0):
   batching vs one at a time: saturation throughput and p50/p99 latency, and
   latency at 1,000 requests/s.
 
-`--workload X` runs one workload alone and prints its full result;
-`--detail PATH` writes every workload's full result to PATH.
+`--workload X` runs one workload alone and prints its full result (also
+`instances`: two-level instancing; `render`: the shading wavefront;
+`ingest`: OBJ and binary PLY read with the reference loaders' rules, then
+uploaded and built); `--detail PATH` writes every workload's full result to
+PATH.
 
 --impl reference times the reference's CPU path (the oracle restatement of
 UniformGridAccStructBuilder + UniformGridAccStruct, compiled here) on the
@@ -1180,6 +1183,64 @@ def run_instances(args, rank, ws, local, dist):
 # shadows), reflection on the plane, refraction on a quarter of the debris,
 # recursion depth 3
 # ---------------------------------------------------------------------------
+def run_ingest(args, rank, ws, local, dist):
+    """Scene ingest: the deforming sphere's mesh (102,400 triangles) written
+    as an indexed OBJ and as a binary little-endian PLY, read back with the
+    reference loaders' rules (rtg_mesh_load, host), then uploaded and built
+    (k = 4).  Host clock, median of `steps` repetitions."""
+    import tempfile
+    import torch
+    from gridrt import lib
+
+    torch.cuda.set_device(local)
+    v, idx, _ = scenes.sphere_mesh()
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        obj = os.path.join(tmp, "sphere.obj")
+        with open(obj, "w") as f:
+            f.write("".join(f"v {float(a)!r} {float(b)!r} {float(c)!r}\n" for a, b, c in v))
+            f.write("".join(f"f {i + 1} {j + 1} {k + 1}\n" for i, j, k in idx))
+        ply = os.path.join(tmp, "sphere.ply")
+        with open(ply, "wb") as f:
+            f.write((f"ply\nformat binary_little_endian 1.0\nelement vertex {len(v)}\nproperty float x\n"
+                     f"property float y\nproperty float z\nelement face {len(idx)}\n"
+                     f"property list uchar int vertex_indices\nend_header\n").encode())
+            f.write(np.ascontiguousarray(v, np.float32).tobytes())
+            rec = np.zeros(len(idx), dtype=np.dtype([("n", "u1"), ("i", "<i4", (3,))]))
+            rec["n"] = 3
+            rec["i"] = idx
+            f.write(rec.tobytes())
+        for name, path in (("obj", obj), ("ply_binary", ply)):
+            size = os.path.getsize(path)
+            load_s, build_s, ntris = [], [], 0
+            for rep in range(max(args.steps, 3) + 1):
+                t0 = time.perf_counter()
+                mv, mt, _, _ = lib.load_mesh(path)
+                t1 = time.perf_counter()
+                s = lib.Scene(local)
+                s.set_geometry(mv, mt)
+                s.build(4)
+                torch.cuda.synchronize()
+                t2 = time.perf_counter()
+                if rep:                                   # the first repetition warms caches and the context
+                    load_s.append(t1 - t0)
+                    build_s.append(t2 - t1)
+                ntris = int(mt.shape[0])
+                del s
+            lm, bm = statistics.median(load_s), statistics.median(build_s)
+            out[name] = {"bytes": size, "triangles": ntris, "load_ms": round(1e3 * lm, 3),
+                         "load_mb_s": round(size / lm / 1e6, 1), "load_mtris_s": round(ntris / lm / 1e6, 2),
+                         "upload_build_ms": round(1e3 * bm, 3)}
+    if rank != 0:
+        return None
+    return {"metric": "Mtriangles/s read (rtg_mesh_load) + upload and grid build ms", "unit": "Mtriangles/s",
+            "value": out["ply_binary"]["load_mtris_s"], "higher_is_better": True, "n_gpus": ws,
+            "steps": args.steps, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "ingest_sphere_102400tri", "k": 4,
+                       "timing": "host clock, median; upload + synchronous build on the device after the load"},
+            "formats": out}
+
+
 def run_render(args, rank, ws, local, dist):
     import torch
     from gridrt import lib
@@ -1505,7 +1566,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gridrt", choices=["gridrt", "reference"])
     ap.add_argument("--workload", default="default",
-                    choices=["default", "deforming", "plain", "batched", "serving", "skewed", "instances", "render"],
+                    choices=["default", "deforming", "plain", "batched", "serving", "skewed", "instances", "render",
+                             "ingest"],
                     help="default: the deforming-mesh headline plus the plain, skewed, batched and serving "
                          "workloads in one line; any other: that workload alone, in full")
     ap.add_argument("--serve-seconds", type=float, default=4.0)
@@ -1526,7 +1588,7 @@ def main():
     args.warmup = max(args.warmup, 3)
     rank, ws, local, dist = _dist()
     single = {"plain": run_plain_small, "batched": run_batched, "serving": run_serving, "skewed": run_skewed,
-              "instances": run_instances, "render": run_render}
+              "instances": run_instances, "render": run_render, "ingest": run_ingest}
     detail = {}
     if args.impl == "reference":
         line = run_reference(args, rank, ws, dist)
