@@ -23,7 +23,6 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <fstream>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -38,6 +37,22 @@ rtg_status mfail(rtg_status s, const std::string& msg) {
     set_last_error(msg);
     return s;
 }
+
+// The whole file in memory (NUL-terminated by std::string): the parsers
+// below scan it in place instead of reading it a value at a time.
+bool read_file(const char* path, std::string& buf) {
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    buf.clear();
+    char chunk[1 << 16];
+    size_t n;
+    while ((n = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.append(chunk, n);
+    const bool ok = !std::ferror(f);
+    std::fclose(f);
+    return ok;
+}
+
+inline bool is_space(char c) { return std::isspace((unsigned char)c) != 0; }
 
 struct Builder {
     std::vector<float> verts;
@@ -92,50 +107,56 @@ struct Builder {
 
 // ---- OBJ -------------------------------------------------------------------
 rtg_status load_obj(const char* path, Builder& B, int64_t* faces) {
-    std::ifstream in(path);
-    if (!in) return mfail(RTG_INVALID_PARAM, std::string("cannot open ") + path);
+    std::string buf;
+    if (!read_file(path, buf)) return mfail(RTG_INVALID_PARAM, std::string("cannot open ") + path);
     std::vector<float> pos;
-    std::string line;
     int64_t f = 0, lineno = 0;
     std::vector<int64_t> corner;
-    while (std::getline(in, line)) {
+    const char* p = buf.c_str();
+    const char* const end = p + buf.size();
+    B.verts.reserve(buf.size() / 8);
+    while (p < end) {
+        const char* nl = static_cast<const char*>(std::memchr(p, '\n', (size_t)(end - p)));
+        const char* le = nl ? nl : end;   // the line is [p, le)
         ++lineno;
-        size_t i = 0;
-        while (i < line.size() && std::isspace((unsigned char)line[i])) ++i;
-        if (i + 1 >= line.size()) continue;
-        if (line[i] == 'v' && std::isspace((unsigned char)line[i + 1])) {
-            const char* p = line.c_str() + i + 1;
-            char* end = nullptr;
-            double x = std::strtod(p, &end);
-            double y = std::strtod(end, &end);
-            double z = std::strtod(end, &end);
+        const char* q = p;
+        while (q < le && is_space(*q)) ++q;
+        if (q + 1 < le && q[0] == 'v' && is_space(q[1])) {
+            char* e = nullptr;
+            const double x = std::strtod(q + 1, &e);
+            const double y = std::strtod(e, &e);
+            const double z = std::strtod(e, &e);
             pos.push_back((float)x);
             pos.push_back((float)y);
             pos.push_back((float)z);
-        } else if (line[i] == 'f' && std::isspace((unsigned char)line[i + 1])) {
-            std::istringstream ss(line.substr(i + 1));
-            std::string tok;
+        } else if (q + 1 < le && q[0] == 'f' && is_space(q[1])) {
             corner.clear();
             const int64_t nv = (int64_t)pos.size() / 3;
-            while (ss >> tok) {
-                const long long r = std::strtoll(tok.c_str(), nullptr, 10);   // "v", "v/t", "v//n", "v/t/n"
-                const long long idx = r > 0 ? r - 1 : nv + r;                  // negative: relative to the end
+            const char* t = q + 1;
+            for (;;) {
+                while (t < le && is_space(*t)) ++t;
+                if (t >= le) break;
+                // one token: "v", "v/t", "v//n" or "v/t/n"; the vertex is its leading integer
+                const long long r = std::strtoll(t, nullptr, 10);
+                const long long idx = r > 0 ? r - 1 : nv + r;   // negative: relative to the end
                 if (r == 0 || idx < 0 || idx >= nv)
                     return mfail(RTG_INVALID_GEOMETRY, "obj line " + std::to_string(lineno) + ": bad vertex index");
                 corner.push_back(idx);
+                while (t < le && !is_space(*t)) ++t;
             }
             if (corner.size() < 3)
                 return mfail(RTG_INVALID_GEOMETRY, "obj line " + std::to_string(lineno) + ": face with < 3 corners");
             // Context::addVertex per corner, then the primitive's triangles
-            const int64_t s = (int64_t)B.verts.size() / 3;
+            const int64_t s0 = (int64_t)B.verts.size() / 3;
             for (int64_t c : corner) B.add_vertex(&pos[3 * c]);
             if (corner.size() == 3) {
-                B.add_triangle(s, s + 1, s + 2, f);
+                B.add_triangle(s0, s0 + 1, s0 + 2, f);
             } else {
-                for (int64_t k = 1; k + 1 < (int64_t)corner.size(); ++k) B.add_triangle(s, s + k, s + k + 1, f);
+                for (int64_t k = 1; k + 1 < (int64_t)corner.size(); ++k) B.add_triangle(s0, s0 + k, s0 + k + 1, f);
             }
             ++f;
         }
+        p = nl ? nl + 1 : end;
     }
     *faces = f;
     return RTG_OK;
@@ -179,24 +200,30 @@ struct PlyElem {
 };
 
 struct PlyReader {
-    std::istream& in;
-    int format;   // 0 ascii, 1 binary little endian, 2 binary big endian
-    explicit PlyReader(std::istream& s, int fmt) : in(s), format(fmt) {}
+    const char* p;     // next byte of the body
+    const char* end;
+    int format;        // 0 ascii, 1 binary little endian, 2 binary big endian
+    bool swap;         // binary byte order differs from the host's
+    PlyReader(const char* begin, const char* e, int fmt) : p(begin), end(e), format(fmt) {
+        const uint16_t one = 1;
+        const bool host_le = *reinterpret_cast<const unsigned char*>(&one) == 1;
+        swap = fmt != 0 && (fmt == 1) != host_le;
+    }
 
     bool read(PlyType t, double* out) {
         if (format == 0) {
-            in >> *out;
-            return (bool)in;
+            char* e = nullptr;
+            *out = std::strtod(p, &e);   // skips leading white space; the buffer is NUL-terminated
+            if (e == p) return false;
+            p = e;
+            return true;
         }
-        unsigned char b[8];
         const int n = ply_size(t);
-        if (!in.read(reinterpret_cast<char*>(b), n)) return false;
-        bool host_le = true;
-        {
-            const uint16_t one = 1;
-            host_le = *reinterpret_cast<const unsigned char*>(&one) == 1;
-        }
-        if ((format == 1) != host_le)
+        if (n == 0 || end - p < n) return false;
+        unsigned char b[8];
+        std::memcpy(b, p, (size_t)n);
+        p += n;
+        if (swap)
             for (int i = 0; i < n / 2; ++i) std::swap(b[i], b[n - 1 - i]);
         switch (t) {
             case P_I8: *out = (double)(int8_t)b[0]; break;
@@ -214,13 +241,24 @@ struct PlyReader {
 };
 
 rtg_status load_ply(const char* path, Builder& B, int64_t* faces) {
-    std::ifstream in(path, std::ios::binary);
-    if (!in) return mfail(RTG_INVALID_PARAM, std::string("cannot open ") + path);
+    std::string buf;
+    if (!read_file(path, buf)) return mfail(RTG_INVALID_PARAM, std::string("cannot open ") + path);
+    // header lines up to end_header; the body starts after its newline
+    const char* cur = buf.c_str();
+    const char* const bend = cur + buf.size();
+    auto next_line = [&](std::string& line) -> bool {
+        if (cur >= bend) return false;
+        const char* nl = static_cast<const char*>(std::memchr(cur, '\n', (size_t)(bend - cur)));
+        const char* le = nl ? nl : bend;
+        line.assign(cur, le);
+        cur = nl ? nl + 1 : bend;
+        return true;
+    };
     std::string line;
-    if (!std::getline(in, line) || line.compare(0, 3, "ply") != 0) return mfail(RTG_INVALID_GEOMETRY, "not a PLY file");
+    if (!next_line(line) || line.compare(0, 3, "ply") != 0) return mfail(RTG_INVALID_GEOMETRY, "not a PLY file");
     int format = -1;
     std::vector<PlyElem> elems;
-    while (std::getline(in, line)) {
+    while (next_line(line)) {
         if (!line.empty() && line.back() == '\r') line.pop_back();
         std::istringstream ss(line);
         std::string kw;
@@ -255,8 +293,17 @@ rtg_status load_ply(const char* path, Builder& B, int64_t* faces) {
         }
     }
     if (format < 0) return mfail(RTG_INVALID_GEOMETRY, "ply: missing or unknown format");
-    PlyReader R(in, format);
+    PlyReader R(cur, bend, format);
     std::vector<float> pos;
+    for (const PlyElem& e : elems) {
+        // room for every vertex and, for triangles, their three new vertices each
+        if (e.name == "vertex" && e.n > 0 && e.n < (int64_t(1) << 31)) pos.reserve(3 * (size_t)e.n);
+        if (e.name == "face" && e.n > 0 && e.n < (int64_t(1) << 31)) {
+            B.verts.reserve(9 * (size_t)e.n);
+            B.tris.reserve(3 * (size_t)e.n);
+            B.face.reserve((size_t)e.n);
+        }
+    }
     std::vector<int64_t> poly;
     int64_t f = 0;
     for (const PlyElem& e : elems) {
