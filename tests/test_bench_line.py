@@ -2,7 +2,8 @@
 default run on a GB300 (tests/fixtures/bench_detail_gb300.json, written by
 `bench.py --detail`), it carries every key of the result-line contract, the
 roofline, CPU-baseline, end-to-end, launch-count and clock objects, one
-small object per further workload, and stays a few KB long."""
+small object per further workload, and stays a few KB long.  The reference
+arm's line, run here on the host cores, names the same metric and workload."""
 import importlib.util
 import json
 import os
@@ -46,3 +47,30 @@ def test_default_line_contract():
     assert back["clocks"]["sm_mhz"] > 0 and isinstance(back["clocks"]["reasons"], list)
     for name in subs:
         assert name in back and back[name].get("value", 0) > 0, name
+
+
+def test_reference_arm_line(oracle):
+    """`bench.py --impl reference` (the reference's CPU path: single-thread
+    grid build and every primary and shadow ray on all host threads) prints
+    one line with the GPU arm's metric, unit and workload, its CPU baseline
+    and an end-to-end object with no device copies."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(HERE, "..", "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=os.path.join(HERE, ".."))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, r.stdout
+    ref = json.loads(lines[0])
+    with open(os.path.join(HERE, "fixtures", "bench_detail_gb300.json")) as f:
+        gpu = json.load(f)["deforming"]
+    assert ref["impl"] == "reference"
+    for key in ("metric", "unit", "higher_is_better", "scaling"):
+        assert ref[key] == gpu[key], key
+    assert ref["config"]["workload"] == gpu["config"]["workload"] and ref["config"]["k"] == gpu["config"]["k"]
+    assert ref["value"] > 0 and ref["steps"] == 1 and ref["warmup"] >= 3
+    cb = ref["cpu_baseline"]
+    assert cb["value"] == ref["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    e = ref["e2e"]
+    assert e["value"] == ref["value"] and e["unit"] == ref["unit"]
+    assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
