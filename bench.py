@@ -9,11 +9,14 @@ Default run (one JSON line, rank 0):
   and 8 in `per_k`); 1024 x 1024 primary camera rays and one shadow ray per
   lit-facing hit, traced as any-hit.  Frames cycle through 20 phases.
   `value` = (primary + shadow rays) / frame time, device-timed with CUDA
-  events on the scene's stream, inputs resident, L2 flushed between frames,
-  each frame (deform + build + trace) replayed from a CUDA graph captured per
-  deformation phase.  `e2e` = the same frames through the public C ABI with
-  host buffers (keyframes from pinned host memory, hits and occlusion copied
-  back every frame), host-clocked.  `cpu_baseline` = the oracle restatement
+  events on the scene's stream, inputs resident.  Two frames are in flight:
+  frames 2j and 2j + 1 each deform, rebuild and trace their own scene (two
+  scenes of the mesh) on their own streams, replayed from one CUDA graph a
+  pair, the L2 flushed before each pair; `one_frame_in_flight` is the same
+  frames one graph a frame on one scene.  `e2e` = the same frames through
+  the public C ABI with host buffers (keyframes from pinned host memory,
+  hits and occlusion copied back every frame, frames alternating over the
+  two scenes), host-clocked.  `cpu_baseline` = the oracle restatement
   of the reference's CPU path on the host cores (single-thread build, every
   ray in 16 x 16 tiles).
 * `cfg0_plain` -- 65,536-triangle plane + debris scene, 512 x 512 rays and
@@ -298,6 +301,17 @@ def run_gpu(args, rank, ws, local, dist):
     d_hits = torch.empty((npix, 4), dtype=torch.int32, device=dev)
     d_occ = torch.empty(npix, dtype=torch.uint8, device=dev)
     d_sr = torch.empty((npix, 8), dtype=torch.float32, device=dev)
+    # a second scene of the same mesh holds the other frame in flight: frames
+    # 2j and 2j + 1 each deform, rebuild and trace their own scene, on their
+    # own streams, so one frame's launch chain runs beside the other's work
+    s2 = lib.Scene(local)
+    s2.set_geometry(v, idx)
+    stream2 = torch.cuda.ExternalStream(s2.stream, device=dev)
+    d_hits2 = torch.empty_like(d_hits)
+    d_occ2 = torch.empty_like(d_occ)
+    d_sr2 = torch.empty_like(d_sr)
+    scene_a = (s, stream, d_hits, d_occ, d_sr)
+    scene_b = (s2, stream2, d_hits2, d_occ2, d_sr2)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
 
@@ -324,24 +338,26 @@ def run_gpu(args, rank, ws, local, dist):
         return None
 
     # capacities for every frame at every k (synchronous builds, untimed)
-    for k in LAMBDAS:
-        for f in range(FRAMES):
-            s.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
-            s.build(k)
+    for sc in (s, s2):
+        for k in LAMBDAS:
+            for f in range(FRAMES):
+                sc.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+                sc.build(k)
 
-    def frame(k, f, order, ev=None):
-        with torch.cuda.stream(stream):
+    def frame(k, f, order, ev=None, on=scene_a):
+        sc, st, hits, occ, sr = on
+        with torch.cuda.stream(st):
             if ev:
-                ev[0].record(stream)
-            s.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
-            s.build_async(k)
+                ev[0].record(st)
+            sc.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+            sc.build_async(k)
             if ev:
-                ev[1].record(stream)
+                ev[1].record(st)
             # primary rays, then each hit's shadow ray (any-hit)
-            s.trace_frame_device(cam, light, d_hits, d_occ, d_sr, order=order)
+            sc.trace_frame_device(cam, light, hits, occ, sr, order=order)
             if ev:
-                ev[2].record(stream)
-                ev[3].record(stream)
+                ev[2].record(st)
+                ev[3].record(st)
 
     # autotune the trace launch shape and ray order per k (results do not
     # depend on them): exhaustive search, each candidate timed on 3 frames
@@ -370,10 +386,12 @@ def run_gpu(args, rank, ws, local, dist):
         _save_autotune(f"deforming_k{k}", allres)
         order = best["order"]
         _apply_tuning(s, best)
+        _apply_tuning(s2, best)
         for w in range(args.warmup):
             frame(k, w % FRAMES, order)
+            frame(k, (w + 1) % FRAMES, order, on=scene_b)
         torch.cuda.synchronize()
-        if s.build_check() != 0:
+        if s.build_check() != 0 or s2.build_check() != 0:
             raise RuntimeError("warm-up build failed: " + lib.load().rtg_last_error().decode())
         evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
         shadow_count = torch.zeros((), dtype=torch.int64, device=dev)
@@ -435,8 +453,54 @@ def run_gpu(args, rank, ws, local, dist):
             raise RuntimeError("graph-replayed build failed: " + lib.load().rtg_last_error().decode())
         g_s = _max_over_ranks(sum(e[0].elapsed_time(e[1]) for e in gevs) / 1e3, dist)
         g_rays = _sum_over_ranks(npix * args.steps + int(gshadow.item()), dist)
-        del graphs
-        per_k[k] = dict(tuning=best, value=g_rays / g_s / 1e6, ms_per_step=1e3 * g_s / args.steps,
+        # two frames in flight: frames 2j and 2j + 1 on the two scenes, forked
+        # and joined inside one graph; the K timed frames are K // 2 such
+        # pairs (and one single frame when K is odd), the L2 flushed before
+        # each
+        pairs = []
+        for j in range(FRAMES // 2):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                fork = torch.cuda.Event()
+                fork.record(stream)
+                stream2.wait_event(fork)
+                frame(k, 2 * j, order)
+                frame(k, 2 * j + 1, order, on=scene_b)
+                join = torch.cuda.Event()
+                join.record(stream2)
+                stream.wait_event(join)
+            pairs.append(g)
+        torch.cuda.synchronize()
+        n_pair = args.steps // 2
+        pevs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(n_pair + args.steps % 2)]
+        pshadow = torch.zeros((), dtype=torch.int64, device=dev)
+        _barrier(dist)
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.mark()
+        for st in range(len(pevs)):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                pevs[st][0].record(stream)
+                if st < n_pair:
+                    pairs[st % (FRAMES // 2)].replay()
+                else:
+                    graphs[(2 * st) % FRAMES].replay()
+                pevs[st][1].record(stream)
+                pshadow += (d_occ != 2).sum()
+                if st < n_pair:
+                    pshadow += (d_occ2 != 2).sum()
+        torch.cuda.synchronize()
+        _barrier(dist)
+        if sampler:
+            sampler.unmark()
+        if s.build_check() != 0 or s2.build_check() != 0:
+            raise RuntimeError("paired build failed: " + lib.load().rtg_last_error().decode())
+        p_s = _max_over_ranks(sum(e[0].elapsed_time(e[1]) for e in pevs) / 1e3, dist)
+        p_rays = _sum_over_ranks(npix * args.steps + int(pshadow.item()), dist)
+        del graphs, pairs
+        per_k[k] = dict(tuning=best, value=p_rays / p_s / 1e6, ms_per_step=1e3 * p_s / args.steps,
+                        one_in_flight_value=g_rays / g_s / 1e6, one_in_flight_ms=1e3 * g_s / args.steps,
                         launches=int(round(per_frame * args.steps)),
                         stream_value=rays_all / total_s / 1e6, stream_ms_per_step=1e3 * total_s / args.steps,
                         build_ms=statistics.median(build_ms), trace_ms=statistics.median(prim_ms),
@@ -490,7 +554,7 @@ def run_gpu(args, rank, ws, local, dist):
     build_s = head["build_ms"] / 1e3
 
     # e2e through the public C ABI with host buffers
-    e2e = run_e2e(args, s, v, idx, nrm, cam, light, best_k, order, dist)
+    e2e = run_e2e(args, (s, s2), v, idx, nrm, cam, light, best_k, order, dist)
 
     if rank != 0:
         return None
@@ -505,8 +569,13 @@ def run_gpu(args, rank, ws, local, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "k": best_k, "ray_order": order, "tuning": head["tuning"], "frames": FRAMES,
                    "triangles": ntris,
-                   "rays_primary": npix, "l2": "flushed between frames (256 MiB write, outside the timed events)",
+                   "rays_primary": npix, "frames_in_flight": 2,
+                   "l2": "flushed before every pair of frames in flight (256 MiB write, outside the timed events)",
                    "parallelism": f"replicas x{ws}"},
+        "one_frame_in_flight": {"value": round(head["one_in_flight_value"], 3),
+                                "ms_per_step": round(head["one_in_flight_ms"], 4),
+                                "how": "the same frames replayed one graph a frame on one scene, the L2 flushed "
+                                       "before each"},
         "build_ms": round(head["build_ms"], 4), "trace_mrays_s": round(head["trace_mrays_s"], 2),
         "per_k": {str(kk): {x: (round(y, 4) if isinstance(y, float) else y) for x, y in d.items() if x != "tuning"}
                   for kk, d in per_k.items()},
@@ -590,7 +659,7 @@ def _save_autotune(name: str, results):
         pass
 
 
-def run_e2e(args, s, v, idx, nrm, cam, light, k, order, dist):
+def run_e2e(args, scs, v, idx, nrm, cam, light, k, order, dist):
     import torch
     from gridrt import lib
     npix = cam.width * cam.height
@@ -598,51 +667,55 @@ def run_e2e(args, s, v, idx, nrm, cam, light, k, order, dist):
     hits = [torch.empty((npix, 4), dtype=torch.int32).pin_memory() for _ in range(2)]
     occ = [torch.empty(npix, dtype=torch.uint8).pin_memory() for _ in range(2)]
     nverts = v.shape[0]
+    copies = [torch.cuda.Stream() for _ in scs]
 
-    copy = torch.cuda.Stream()
-
-    # a frame: its keyframe (staged during the previous frame) is built, the
-    # next keyframe is uploaded on a copy stream while this frame traces, and
+    # frame f runs on scene f % 2 (two scenes, the same mesh: two frames in
+    # flight on the device, each on its own streams).  A frame builds its
+    # keyframe (staged during that scene's previous frame), uploads the
+    # scene's next keyframe (f + 2) on a copy stream while it traces, and its
     # hits + occlusion are copied back on the scene's copy stream while the
     # next frame builds and traces; the host waits for frame f's results
-    # after enqueuing frame f + 1 (two frames in flight, alternating host
-    # buffers)
-    def enqueue(f, i):
-        s.build_async(k)
-        s.stage_vertices(host_verts[(f + 1) % FRAMES], nverts, copy.cuda_stream)
-        return s.trace_frame_async(cam, light, hits[i % 2], occ[i % 2], order=order)
+    # after enqueuing frame f + 1 (host buffers alternate with the scenes)
+    def enqueue(f):
+        sc = scs[f % 2]
+        sc.build_async(k)
+        sc.stage_vertices(host_verts[(f + 2) % FRAMES], nverts, copies[f % 2].cuda_stream)
+        return sc, sc.trace_frame_async(cam, light, hits[f % 2], occ[f % 2], order=order)
 
     def run(first, count):
         prev = None
         for i in range(count):
-            t = enqueue((first + i) % FRAMES, i)
+            t = enqueue((first + i) % FRAMES)
             if prev is not None:
-                s.trace_frame_wait(prev)
+                prev[0].trace_frame_wait(prev[1])
             prev = t
         if prev is not None:
-            s.trace_frame_wait(prev)
+            prev[0].trace_frame_wait(prev[1])
 
     # shadow rays per frame (deterministic per frame), counted outside the timed loop
     shadow_of = []
-    s.stage_vertices(host_verts[0], nverts, copy.cuda_stream)
+    for j, sc in enumerate(scs):
+        sc.stage_vertices(host_verts[j], nverts, copies[j].cuda_stream)
     for f in range(FRAMES):
-        s.trace_frame_wait(enqueue(f, 0))
-        shadow_of.append(int((occ[0].numpy() != 2).sum()))
-    run(0, args.warmup)           # frame 0's keyframe was staged by the last counted frame
+        sc, t = enqueue(f)
+        sc.trace_frame_wait(t)
+        shadow_of.append(int((occ[f % 2].numpy() != 2).sum()))
+    run(0, args.warmup)           # frames 0 and 1's keyframes were staged by the last counted frames
     _barrier(dist)
     t0 = time.perf_counter()
     run(args.warmup, args.steps)
     t = _max_over_ranks(time.perf_counter() - t0, dist)
-    if s.build_check() != 0:
+    if any(sc.build_check() != 0 for sc in scs):
         raise RuntimeError("e2e build failed: " + lib.load().rtg_last_error().decode())
     shadow = sum(shadow_of[(args.warmup + st) % FRAMES] for st in range(args.steps))
     rays = _sum_over_ranks(npix * args.steps + shadow, dist)
     return {"value": round(rays / t / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(nverts * 12),
             "d2h_bytes_per_step": int(npix * 17), "ms_per_step": round(1e3 * t / args.steps, 3),
-            "how": "host clock over the frame loop: per frame rtg_scene_build_async + rtg_scene_stage_vertices "
-                   "(next keyframe from pinned host memory on a copy stream) + rtg_trace_frame_async (hits and "
-                   "occlusion copied to pinned host memory on the scene's copy stream), and rtg_trace_frame_wait "
-                   "for the previous frame's results; the clock stops after the last frame's results are on the host"}
+            "how": "host clock over the frame loop, frames alternating over two scenes of the mesh: per frame "
+                   "rtg_scene_build_async + rtg_scene_stage_vertices (that scene's next keyframe from pinned host "
+                   "memory on a copy stream) + rtg_trace_frame_async (hits and occlusion copied to pinned host "
+                   "memory on the scene's copy stream), and rtg_trace_frame_wait for the previous frame's results; "
+                   "the clock stops after the last frame's results are on the host"}
 
 
 # ---------------------------------------------------------------------------
@@ -1493,13 +1566,20 @@ def compact_line(full: dict, subs: dict) -> dict:
                               "higher_is_better", "scaling", "vs_baseline", "dtype", "data")}
     cfg = full["config"]
     c["config"] = {"workload": cfg["workload"], "k": cfg["k"], "frames": cfg["frames"], "triangles": cfg["triangles"],
-                   "rays_primary": cfg["rays_primary"], "l2": "flushed between frames (256 MiB write)",
+                   "rays_primary": cfg["rays_primary"], "frames_in_flight": cfg.get("frames_in_flight", 1),
+                   "l2": ("flushed before every pair of frames in flight (256 MiB write)"
+                          if cfg.get("frames_in_flight", 1) == 2 else "flushed between frames (256 MiB write)"),
                    "parallelism": cfg["parallelism"], "tuning": _tune_str(cfg["tuning"]),
                    "tuned_by": full.get("autotune", {}).get(str(cfg["k"]), {}).get("source")}
+    if "one_frame_in_flight" in full:
+        o = full["one_frame_in_flight"]
+        c["one_frame_in_flight"] = {"value": _r(o["value"], 1), "ms_per_step": o["ms_per_step"]}
     c["build_ms"] = _r(full["build_ms"], 4)
     c["trace_mrays_s"] = _r(full["trace_mrays_s"], 1)
     c["per_k"] = {k: {"value": _r(v["value"], 1), "build_ms": _r(v["build_ms"], 4),
-                      "stream_value": _r(v["stream_value"], 1)} for k, v in full["per_k"].items()}
+                      "stream_value": _r(v["stream_value"], 1),
+                      **({"one_in_flight": _r(v["one_in_flight_value"], 1)} if "one_in_flight_value" in v else {})}
+                  for k, v in full["per_k"].items()}
     rf = full["roofline"]
     c["roofline"] = {"bound": rf["bound"], "achieved": rf["achieved"], "peak": rf["peak"], "unit": rf["unit"],
                      "frac": rf["frac"], "traffic": rf["traffic"], "peak_source": rf["peak_source"],

@@ -47,6 +47,13 @@ def test_default_line_contract():
     assert back["clocks"]["sm_mhz"] > 0 and isinstance(back["clocks"]["reasons"], list)
     for name in subs:
         assert name in back and back[name].get("value", 0) > 0, name
+    # two frames in flight: the line also carries the one-frame figure
+    full = dict(d["deforming"], one_frame_in_flight={"value": 3478.3, "ms_per_step": 0.3792})
+    full["config"] = dict(full["config"], frames_in_flight=2)
+    two = bench.compact_line(full, subs)
+    assert two["config"]["frames_in_flight"] == 2 and "pair" in two["config"]["l2"]
+    assert two["one_frame_in_flight"]["value"] == 3478.3
+    assert len(json.dumps(two, separators=(",", ":"))) < 4096
 
 
 def test_reference_arm_line(oracle):
