@@ -385,3 +385,101 @@ def test_frame_async_matches_frame(gridlib):
     assert (ref[0][1] != 2).sum() > 0          # the frames have shadow rays
     with pytest.raises(gridlib.GridRTError):
         s.trace_frame_wait(7)
+
+
+def test_two_frames_in_flight_match_one_at_a_time(gridlib):
+    """Two scenes of one mesh with a frame in flight on each give exactly the
+    hits and occlusion of the same frames one at a time on one scene: frames
+    2j and 2j + 1 deformed, rebuilt and traced on their scenes' own streams
+    as two branches of one CUDA graph, and frames alternating over the two
+    scenes with staged host keyframes and asynchronous read-back."""
+    import torch
+    v, idx, nrm = scenes.sphere_mesh()
+    cam = scenes.deforming_sphere_camera(512, 512)
+    n = cam.width * cam.height
+    light = scenes.SPHERE_LIGHT
+    dev = torch.device("cuda", 0)
+    d_base = torch.from_numpy(v).to(dev)
+    d_nrm = torch.from_numpy(nrm).to(dev)
+
+    def make():
+        s = gridlib.Scene(0)
+        s.set_geometry(v, idx)
+        return (s, torch.cuda.ExternalStream(s.stream, device=dev),
+                torch.empty((n, 4), dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
+                torch.empty((n, 8), dtype=torch.float32, device=dev))
+
+    a, b = make(), make()
+    for sc in (a[0], b[0]):                    # capacities for every frame
+        for f in range(4):
+            sc.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+            sc.build(4)
+
+    def frame(on, f):
+        sc, st, hits, occ, sr = on
+        with torch.cuda.stream(st):
+            sc.deform(d_base, d_nrm, 0.05, 3.0, 0.3 * f)
+            sc.build_async(4)
+            sc.trace_frame_device(cam, light, hits, occ, sr, order="morton8")
+
+    ref = []
+    for f in range(4):
+        frame(a, f)
+        torch.cuda.synchronize()
+        ref.append((a[2].cpu().numpy(), a[3].cpu().numpy()))
+    assert (ref[0][1] != 2).sum() > 0          # the frames have shadow rays
+    for j in range(2):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=a[1]):
+            fork = torch.cuda.Event()
+            fork.record(a[1])
+            b[1].wait_event(fork)
+            frame(a, 2 * j)
+            frame(b, 2 * j + 1)
+            join = torch.cuda.Event()
+            join.record(b[1])
+            a[1].wait_event(join)
+        for _ in range(2):
+            g.replay()
+            torch.cuda.synchronize()
+            for on, f in ((a, 2 * j), (b, 2 * j + 1)):
+                assert np.array_equal(on[2].cpu().numpy(), ref[f][0]), f
+                assert np.array_equal(on[3].cpu().numpy(), ref[f][1]), f
+        del g
+    assert a[0].build_check() == 0 and b[0].build_check() == 0
+
+    # host keyframes, frames alternating over the two scenes
+    nv = v.shape[0]
+    keys = [torch.from_numpy(np.ascontiguousarray(scenes.deform(v, nrm, f), np.float32)).pin_memory()
+            for f in range(4)]
+    href = []
+    for f in range(4):
+        a[0].update_vertices(keys[f].numpy(), nv, False)
+        a[0].build(4)
+        h, o = np.empty((n, 4), np.int32), np.empty(n, np.uint8)
+        a[0].trace_frame(cam, light, h, o, order="morton8")
+        href.append((h, o))
+    scs = (a[0], b[0])
+    copies = [torch.cuda.Stream() for _ in scs]
+    hits = [torch.empty((n, 4), dtype=torch.int32).pin_memory() for _ in range(2)]
+    occ = [torch.empty(n, dtype=torch.uint8).pin_memory() for _ in range(2)]
+    for j, sc in enumerate(scs):
+        sc.stage_vertices(keys[j], nv, copies[j].cuda_stream)
+
+    def check(f):
+        assert np.array_equal(hits[f % 2].numpy(), href[f % 4][0]), f
+        assert np.array_equal(occ[f % 2].numpy(), href[f % 4][1]), f
+
+    prev = None
+    for f in range(9):
+        sc = scs[f % 2]
+        sc.build_async(4)
+        sc.stage_vertices(keys[(f + 2) % 4], nv, copies[f % 2].cuda_stream)
+        t = (sc, sc.trace_frame_async(cam, light, hits[f % 2], occ[f % 2], order="morton8"), f)
+        if prev is not None:
+            prev[0].trace_frame_wait(prev[1])
+            check(prev[2])
+        prev = t
+    prev[0].trace_frame_wait(prev[1])
+    check(prev[2])
+    assert a[0].build_check() == 0 and b[0].build_check() == 0
