@@ -1036,21 +1036,30 @@ def run_skewed(args, rank, ws, local, dist):
     d_hits = torch.empty((npix, 4), dtype=torch.int32, device=dev)
     d_sec = torch.empty((npix, 8), dtype=torch.float32, device=dev)
     d_hits2 = torch.empty((npix, 4), dtype=torch.int32, device=dev)
+    # a second scene of the same triangles holds the other step in flight
+    s2 = lib.Scene(local)
+    s2.set_geometry(sc.verts, sc.idx)
+    stream2 = torch.cuda.ExternalStream(s2.stream, device=dev)
+    d_sec_b = torch.empty_like(d_sec)
+    scene_a = (s, stream, d_hits, d_sec, d_hits2)
+    scene_b = (s2, stream2, torch.empty_like(d_hits), d_sec_b, torch.empty_like(d_hits2))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for k in LAMBDAS:
         s.build(k)          # capacities for every k (untimed)
+        s2.build(k)
 
-    def step(k, seed, order, ev=None):
-        with torch.cuda.stream(stream):
+    def step(k, seed, order, ev=None, on=scene_a):
+        g, st, hits, sec, hits2 = on
+        with torch.cuda.stream(st):
             if ev:
-                ev[0].record(stream)
-            s.build_async(k)
+                ev[0].record(st)
+            g.build_async(k)
             if ev:
-                ev[1].record(stream)
-            s.trace_camera_diffuse_device(cam, seed, d_hits, d_sec, order=order)
-            s.trace_nearest_device(d_sec, npix, d_hits2)
+                ev[1].record(st)
+            g.trace_camera_diffuse_device(cam, seed, hits, sec, order=order)
+            g.trace_nearest_device(sec, npix, hits2)
             if ev:
-                ev[2].record(stream)
+                ev[2].record(st)
 
     def measure(cfg):
         _apply_tuning(s, cfg)
@@ -1070,11 +1079,13 @@ def run_skewed(args, rank, ws, local, dist):
         best, allres = autotune.search(measure, space=space, reps=2)
         _save_autotune("skewed", allres)
     _apply_tuning(s, best)
+    _apply_tuning(s2, best)
     k, order = best["k"], best["order"]
     for w in range(args.warmup):
         step(k, 100 + w, order)
+        step(k, 200 + w, order, on=scene_b)
     torch.cuda.synchronize()
-    if s.build_check() != 0:
+    if s.build_check() != 0 or s2.build_check() != 0:
         raise RuntimeError("warm-up build failed: " + lib.load().rtg_last_error().decode())
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     nsec = torch.zeros((), dtype=torch.int64, device=dev)
@@ -1094,11 +1105,50 @@ def run_skewed(args, rank, ws, local, dist):
     torch.cuda.synchronize()
     if sampler:
         sampler.unmark()
-        sampler.stop()
     build_ms = [e[0].elapsed_time(e[1]) for e in evs]
     step_ms = [e[0].elapsed_time(e[2]) for e in evs]
-    t_ms = _max_over_ranks(sum(step_ms), dist)
-    rays = _sum_over_ranks(npix * args.steps + int(nsec.item()), dist)
+    one_ms = _max_over_ranks(sum(step_ms), dist)
+    one_rays = _sum_over_ranks(npix * args.steps + int(nsec.item()), dist)
+
+    # two steps in flight: steps 2j and 2j + 1 on the two scenes, each on its
+    # own streams (forked from and joined back to the first scene's stream),
+    # so one step's build runs beside the other's trace; the same K steps,
+    # the L2 flushed before each pair
+    n_pair = args.steps // 2
+    pevs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(n_pair + args.steps % 2)]
+    fork = [torch.cuda.Event() for _ in pevs]
+    join = [torch.cuda.Event() for _ in pevs]
+    nsec2 = torch.zeros((), dtype=torch.int64, device=dev)
+    _barrier(dist)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.mark()
+    for st in range(len(pevs)):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            pevs[st][0].record(stream)
+        if st < n_pair:
+            fork[st].record(stream)
+            stream2.wait_event(fork[st])
+            step(k, 1000 + 2 * st, order)
+            step(k, 1000 + 2 * st + 1, order, on=scene_b)
+            join[st].record(stream2)
+            stream.wait_event(join[st])
+        else:
+            step(k, 1000 + 2 * st, order)
+        with torch.cuda.stream(stream):
+            pevs[st][1].record(stream)
+            nsec2 += (d_sec[:, 7] > 0).sum()
+            if st < n_pair:
+                nsec2 += (d_sec_b[:, 7] > 0).sum()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.unmark()
+        sampler.stop()
+    if s.build_check() != 0 or s2.build_check() != 0:
+        raise RuntimeError("paired build failed: " + lib.load().rtg_last_error().decode())
+    t_ms = _max_over_ranks(sum(e[0].elapsed_time(e[1]) for e in pevs), dist)
+    rays = _sum_over_ranks(npix * args.steps + int(nsec2.item()), dist)
 
     # traversal counters of one step (primary, then secondary rays) for the
     # algorithmic bytes: 16 B hit + 32 B secondary ray written per primary
@@ -1136,7 +1186,10 @@ def run_skewed(args, rank, ws, local, dist):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "skewed_density_1048576tri_1024x1024_diffuse", "k": k, "ray_order": order,
                    "tuning": best, "triangles": sc.ntris, "rays_per_step": round(rays / args.steps / ws),
-                   "l2": "flushed between steps (256 MiB write, outside the timed events)"},
+                   "steps_in_flight": 2,
+                   "l2": "flushed before every pair of steps in flight (256 MiB write, outside the timed events)"},
+        "one_step_in_flight": {"value": round(one_rays / one_ms / 1e3, 3), "ms_per_step": round(one_ms / args.steps, 4),
+                               "how": "the same steps one at a time on one scene, the L2 flushed before each"},
         "build_ms": round(statistics.median(build_ms), 4),
         "trace_ms": round(trace_ms, 4),
         "counters": {"primary": c1, "secondary": c2,
@@ -1610,6 +1663,7 @@ def compact_skewed(d: dict) -> dict:
             "ms_per_step": d["ms_per_step"], "build_ms": d["build_ms"], "trace_ms": d["trace_ms"],
             "rays_per_step": d["config"]["rays_per_step"], "tests_per_ray": d["counters"]["tests_per_ray"],
             "roofline_frac": d["roofline"]["frac"], "tuning": _tune_str(d["config"]["tuning"]),
+            **({"one_in_flight": _r(d["one_step_in_flight"]["value"], 1)} if "one_step_in_flight" in d else {}),
             "fp64_max": {g: [_r(err[g]["t_rel"]["max"], 8), _r(err[g]["u_abs"]["max"], 8),
                              _r(err[g]["v_abs"]["max"], 8)] for g in ("primary", "secondary")}}
 

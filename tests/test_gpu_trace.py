@@ -483,3 +483,55 @@ def test_two_frames_in_flight_match_one_at_a_time(gridlib):
     prev[0].trace_frame_wait(prev[1])
     check(prev[2])
     assert a[0].build_check() == 0 and b[0].build_check() == 0
+
+
+def test_two_dense_cluster_scenes_in_flight(gridlib):
+    """Two scenes of the dense-cluster scene, each rebuilt and traced
+    (camera rays writing diffuse secondaries, then the secondaries) on its
+    own stream at the same time, give exactly the results of the same steps
+    one at a time: cluster sorts, deferral and the staged block-per-ray pass
+    included."""
+    import torch
+    sc, k = scenes.skewed_density(n=1 << 16), 4
+    cam = scenes.skewed_density_camera(256, 256)
+    n = cam.width * cam.height
+    dev = torch.device("cuda", 0)
+
+    def make():
+        s = gridlib.Scene(0)
+        s.set_geometry(sc.verts, sc.idx)
+        s.build(k)
+        s.set_tuning(heavy_cell=32, heavy_lanes=16, refill=16, cell_records=True)
+        return (s, torch.cuda.ExternalStream(s.stream, device=dev), torch.empty((n, 4), dtype=torch.int32, device=dev),
+                torch.empty((n, 8), dtype=torch.float32, device=dev), torch.empty((n, 4), dtype=torch.int32, device=dev))
+
+    def step(on, seed):
+        g, st, hits, sec, hits2 = on
+        with torch.cuda.stream(st):
+            g.build_async(k)
+            g.trace_camera_diffuse_device(cam, seed, hits, sec, order="morton8")
+            g.trace_nearest_device(sec, n, hits2)
+
+    def result(on):
+        return [x.cpu().numpy().view(np.uint32) for x in on[2:]]
+
+    a, b = make(), make()
+    ref = {}
+    for seed in range(1, 5):
+        step(a, seed)
+        torch.cuda.synchronize()
+        ref[seed] = result(a)
+    assert (ref[1][0][:, 0].view(np.int32) >= 0).sum() > 0
+    for j in range(2):
+        fork, join = torch.cuda.Event(), torch.cuda.Event()
+        fork.record(a[1])
+        b[1].wait_event(fork)
+        step(a, 1 + 2 * j)
+        step(b, 2 + 2 * j)
+        join.record(b[1])
+        a[1].wait_event(join)
+        torch.cuda.synchronize()
+        for on, seed in ((a, 1 + 2 * j), (b, 2 + 2 * j)):
+            for got, want in zip(result(on), ref[seed]):
+                assert np.array_equal(got, want), seed
+    assert a[0].build_check() == 0 and b[0].build_check() == 0
