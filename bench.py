@@ -281,6 +281,23 @@ def run_reference(args, rank, ws, dist):
 # ---------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------
+def _pair_ms(torch, stream, stream2, enqueue):
+    """Device time of the work `enqueue` puts on two streams: the second
+    stream forked from the first before it and joined back after it, CUDA
+    events on the first around both."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fork, join = torch.cuda.Event(), torch.cuda.Event()
+    e0.record(stream)
+    fork.record(stream)
+    stream2.wait_event(fork)
+    enqueue()
+    join.record(stream2)
+    stream.wait_event(join)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
 def run_gpu(args, rank, ws, local, dist):
     import torch
     from gridrt import lib
@@ -359,18 +376,21 @@ def run_gpu(args, rank, ws, local, dist):
                 ev[2].record(st)
                 ev[3].record(st)
 
+    def pair_ms(enqueue):
+        return _pair_ms(torch, stream, stream2, enqueue)
+
     # autotune the trace launch shape and ray order per k (results do not
     # depend on them): exhaustive search, each candidate timed on 3 frames
     from gridrt import autotune
 
     def tune_k(k):
+        # each candidate timed as the headline runs: a pair of frames in
+        # flight on the two scenes (after one untimed frame)
         def measure(cfg):
             _apply_tuning(s, cfg)
-            evs = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            _apply_tuning(s2, cfg)
             frame(k, 0, cfg["order"])
-            frame(k, 1, cfg["order"], evs)
-            torch.cuda.synchronize()
-            return evs[1].elapsed_time(evs[3])
+            return pair_ms(lambda: (frame(k, 1, cfg["order"]), frame(k, 2, cfg["order"], on=scene_b)))
         return autotune.search(measure, reps=3)
 
     tuned = {}
@@ -776,17 +796,16 @@ def run_plain_small(args, rank, ws, local, dist):
                 ev[2].record(st)
 
     # the autotuner's launch shape and ray order for this step (results do
-    # not depend on them), each candidate timed on one step after one untimed
+    # not depend on them), each candidate timed on a pair of steps in flight
+    # on the two scenes, after one untimed step
     from gridrt import autotune
 
     def measure(cfg):
         _apply_tuning(s, cfg)
+        _apply_tuning(s2, cfg)
         order[0] = cfg["order"]
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         step()
-        step(ev)
-        torch.cuda.synchronize()
-        return ev[0].elapsed_time(ev[2])
+        return _pair_ms(torch, stream, stream2, lambda: (step(), step(on=scene_b)))
 
     fixed = _parse_tuning(args.fixed_tuning)
     if fixed:
