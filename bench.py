@@ -1120,13 +1120,15 @@ def run_skewed(args, rank, ws, local, dist):
             if ev:
                 ev[2].record(st)
 
+    # each candidate timed as the workload runs: a pair of steps in flight on
+    # the two scenes (after one untimed step)
     def measure(cfg):
         _apply_tuning(s, cfg)
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        step(cfg["k"], 1, cfg["order"])
-        step(cfg["k"], 2, cfg["order"], ev)
-        torch.cuda.synchronize()
-        return ev[0].elapsed_time(ev[2])
+        _apply_tuning(s2, cfg)
+        k = cfg["k"]
+        step(k, 1, cfg["order"])
+        return _pair_ms(torch, stream, stream2,
+                        lambda: (step(k, 2, cfg["order"]), step(k, 3, cfg["order"], on=scene_b)))
 
     fixed = _parse_tuning(args.fixed_tuning)
     if fixed:
