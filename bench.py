@@ -380,12 +380,11 @@ def run_gpu(args, rank, ws, local, dist):
         return _pair_ms(torch, stream, stream2, enqueue)
 
     # autotune the trace launch shape and ray order per k (results do not
-    # depend on them): exhaustive search, each candidate timed on 3 frames
+    # depend on them); each candidate is timed as the headline runs: a pair
+    # of frames in flight on the two scenes, after one untimed frame
     from gridrt import autotune
 
     def tune_k(k):
-        # each candidate timed as the headline runs: a pair of frames in
-        # flight on the two scenes (after one untimed frame)
         def measure(cfg):
             _apply_tuning(s, cfg)
             _apply_tuning(s2, cfg)
