@@ -81,3 +81,35 @@ def test_reference_arm_line(oracle):
     e = ref["e2e"]
     assert e["value"] == ref["value"] and e["unit"] == ref["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_tuning_text_round_trip():
+    """--fixed-tuning text parses into every launch-shape setting (unnamed
+    ones at the library's defaults), and the line's short form names each."""
+    bench = _bench()
+    text = ("k=4,order=morton8,empty_run=4,persistent=1,heavy_cell=32,heavy_lanes=16,cell_records=1,refill=16,"
+            "block=256,lanes=2")
+    cfg = bench._parse_tuning(text)
+    assert cfg == {"k": 4, "order": "morton8", "empty_run": 4, "persistent": True, "heavy_cell": 32,
+                   "heavy_lanes": 16, "cell_records": True, "refill": 16, "block": 256, "lanes": 2}
+    assert bench._tune_str(cfg) == "morton8/er4/p1/h32x16/r16/c1/b256/l2"
+    short = bench._parse_tuning("k=2,order=scanline")
+    assert short["persistent"] is False and short["cell_records"] is False
+    assert (short["block"], short["lanes"], short["heavy_lanes"], short["refill"]) == (128, 1, 32, 0)
+    assert bench._parse_tuning("") is None and bench._tune_str(None) == ""
+
+
+def test_cpu_tile_order():
+    """The CPU arms trace rays in 16 x 16 pixel tiles, row of tiles after row
+    of tiles (the reference TiledRenderer's schedule): a permutation of the
+    scanline indices whose every run of 256 is one tile."""
+    import numpy as np
+    bench = _bench()
+    w, h = 64, 32
+    order = bench._tile_order(w, h)
+    assert np.array_equal(np.sort(order), np.arange(w * h))
+    for t in range(w * h // 256):
+        run = order[256 * t:256 * (t + 1)]
+        x, y = run % w, run // w
+        assert x.max() - x.min() == 15 and y.max() - y.min() == 15
+        assert (x.min(), y.min()) == ((t % (w // 16)) * 16, (t // (w // 16)) * 16)
