@@ -387,12 +387,15 @@ def test_frame_async_matches_frame(gridlib):
         s.trace_frame_wait(7)
 
 
-def test_two_frames_in_flight_match_one_at_a_time(gridlib):
+@pytest.mark.parametrize("persistent", [True, False])
+def test_two_frames_in_flight_match_one_at_a_time(gridlib, persistent):
     """Two scenes of one mesh with a frame in flight on each give exactly the
     hits and occlusion of the same frames one at a time on one scene: frames
     2j and 2j + 1 deformed, rebuilt and traced on their scenes' own streams
     as two branches of one CUDA graph, and frames alternating over the two
-    scenes with staged host keyframes and asynchronous read-back."""
+    scenes with staged host keyframes and asynchronous read-back.  With
+    persistent trace grids and with one-shot grids of 64-thread blocks (whose
+    blocks from the two frames share the SMs)."""
     import torch
     v, idx, nrm = scenes.sphere_mesh()
     cam = scenes.deforming_sphere_camera(512, 512)
@@ -405,6 +408,10 @@ def test_two_frames_in_flight_match_one_at_a_time(gridlib):
     def make():
         s = gridlib.Scene(0)
         s.set_geometry(v, idx)
+        if persistent:
+            s.set_tuning(persistent=True)
+        else:
+            s.set_tuning(persistent=False, block=64, heavy_cell=48)
         return (s, torch.cuda.ExternalStream(s.stream, device=dev),
                 torch.empty((n, 4), dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
                 torch.empty((n, 8), dtype=torch.float32, device=dev))
