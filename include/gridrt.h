@@ -464,7 +464,12 @@ rtg_status rtg_serve_run(const rtg_scene* scenes, int32_t nscenes, const rtg_req
 
 /* Trace launch shape for this scene (results never depend on it):
  *   RTG_TUNE_EMPTY_RUN   empty cells a ray may walk per loop turn: 2, 4, 8, 16 (default 4)
- *   RTG_TUNE_PERSISTENT  1: persistent warps claim ray batches (default); 0: one batch per warp
+ *   RTG_TUNE_PERSISTENT  1: persistent warps claim ray batches (default); 0: one batch per warp.
+ *                        A persistent launch holds every SM's slots until it ends; a one-shot
+ *                        launch's blocks retire as they finish, so traces of two scenes in
+ *                        flight on their own streams share the SMs (1024^2 frames two in
+ *                        flight: 3,846 Mrays/s persistent, 4,392 one-shot with blocks of 64;
+ *                        one frame at a time persistent is the faster, ~3,470 against 3,367)
  *   RTG_TUNE_CELL_RECORDS 1: builds also store the triangle records in cell-list order
  *                        (48 B per reference) so traces skip the id indirection; from the next build
  *   RTG_TUNE_HEAVY_CELL  n > 0: a ray that meets a cell list longer than n is finished by a
